@@ -1,0 +1,323 @@
+"""Benchmark: batched FP64 Cholesky solve on GB300 (BLAST potrf + two trsm).
+
+Workload (one "step"): 50,000 SPD matrices n = 48, A = G*G^T + 48*I with G i.i.d. N(0,1),
+B (48 x 8) i.i.d. N(0,1); potrf(A, L) then L*Y = B, L^T*X = Y, all binary64, inputs resident in
+HBM (1.07 GB of inputs, larger than the 129 MB L2, so no L2 flush is needed between steps).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line. `value` is matrices/s measured with CUDA events on the launching stream
+(max over ranks); `e2e` is the same metric through the public API with pinned host buffers and
+the host<->device copies inside the timed region; `roofline` is the binary64 issue bound of the
+dominant kernel; `cpu_baseline` times the CPU restatement of BLAST's algorithm on this host.
+With --impl reference the CPU restatement of BLAST (one instance per call, instances spread over
+all host cores with OpenMP) is timed on the same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N, NRHS, BATCH = 48, 8, 50_000
+FLOPS_PER = N ** 3 / 3 + N ** 2 / 2 + N / 6 + 2 * N * N * NRHS          # 74,888
+BYTES_PER = 8 * (N * (N + 1) // 2 * 2 + 2 * N * NRHS)                     # 24,960 (lower A in, L out, B in, X out)
+METRIC = "matrices/s, GFLOP/s on 1 GB300: FP64 vs mixed+IR batched potrf at 1e-12 bwd err"
+WORKLOAD = "FP64 batched Cholesky solve: potrf + 2 trsm, 50,000 SPD n=48 (A = G*G^T + 48*I), B 48x8"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.out = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        if not self.out:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out.strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_inputs(batch: int, seed: int, device):
+    """Seeded synthetic Cholesky-solve batch, generated on the device."""
+    import torch
+
+    import blast_gb300 as bg
+
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    G = torch.randn(batch, N, N, generator=g, device=device, dtype=torch.float64)
+    A = bg.col_major((batch,), N, N, device)
+    torch.baddbmm(torch.eye(N, device=device, dtype=torch.float64).mul_(N), G, G.mT, out=A.mT)
+    del G
+    B = bg.col_major((batch,), N, NRHS, device)
+    B.copy_(torch.randn(batch, N, NRHS, generator=g, device=device, dtype=torch.float64))
+    return A, B
+
+
+def peak_fp64_tflops() -> float:
+    """Binary64 FMA throughput of this GPU, measured by the library's probe kernel."""
+    import ctypes
+
+    import torch
+
+    from blast_gb300 import _lib
+
+    out = ctypes.c_double(0.0)
+    _lib.call("blastgpu_probe_fp64_tflops", ctypes.byref(out), torch.cuda.current_stream().cuda_stream)
+    return out.value
+
+
+def load_traffic():
+    p = ROOT / "profiles" / "posv_n48_traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            return None
+    return None
+
+
+def cpu_baseline(max_seconds: float = 12.0):
+    """The oracle's BLAST restatement on this host's cores, on a bounded sample."""
+    import numpy as np
+
+    from oracle import oracle as orc
+
+    threads = orc.max_threads()
+    rng = np.random.default_rng(7)
+    sample = 4000
+    G = rng.standard_normal((sample, N, N))
+    A = G @ np.swapaxes(G, 1, 2) + N * np.eye(N)
+    B = rng.standard_normal((sample, N, NRHS))
+    prep = orc.posv_prepare(A, B)
+    orc.posv_run(prep, threads)  # warm-up
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        orc.posv_run(prep, threads)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= max_seconds / 4 or reps >= 50:
+            break
+    rate = reps * sample / el
+    return {"value": rate, "unit": "matrices/s", "cores": threads, "kind": "port",
+            "gflops": rate * FLOPS_PER / 1e9,
+            "sample": f"{reps} x {sample} matrices of the same workload (n=48, 8 RHS), "
+                      f"one instance per call, OpenMP over {threads} threads, {el:.2f} s"}
+
+
+def run_reference(args):
+    ws, rank = _dist()
+    if rank != 0:
+        return
+    base = cpu_baseline(max_seconds=8.0 * max(1, args.steps) / 10)
+    line = {"metric": METRIC, "value": base["value"], "unit": "matrices/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": BATCH / base["value"] * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "batch": BATCH, "n": N, "nrhs": NRHS},
+            "gflops": base["gflops"],
+            "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": base["value"], "unit": "matrices/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    import blast_gb300 as bg
+    from blast_gb300 import _lib
+
+    ws, rank = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    stream = torch.cuda.current_stream()
+
+    A, B = make_inputs(BATCH, 1234 + rank, dev)
+    L = bg.col_major((BATCH,), N, N, dev)
+    X = bg.col_major((BATCH,), N, NRHS, dev)
+
+    def step():
+        return bg.posv(A, L, B, X)
+
+    for _ in range(max(args.warmup, 3)):
+        info = step()
+    torch.cuda.synchronize()
+    assert int(info.abs().sum()) == 0
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = _lib.launch_count()
+    barrier()
+    with ClockSampler(local) as clocks:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    launches = _lib.launch_count() - launches0
+    ms = e0.elapsed_time(e1) / args.steps
+    if ws > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # End to end through the public API: pinned host A, B -> device -> posv -> L, X to host.
+    hA = torch.empty(A.mT.shape, dtype=torch.float64, pin_memory=True)
+    hB = torch.empty(B.mT.shape, dtype=torch.float64, pin_memory=True)
+    hA.copy_(A.mT)
+    hB.copy_(B.mT)
+    hL = torch.empty_like(hA, pin_memory=True)
+    hX = torch.empty_like(hB, pin_memory=True)
+    dA, dB = A, B
+
+    def e2e_step():
+        dA.mT.copy_(hA, non_blocking=True)
+        dB.mT.copy_(hB, non_blocking=True)
+        bg.posv(dA, L, dB, X)
+        hL.copy_(L.mT, non_blocking=True)
+        hX.copy_(X.mT, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_steps = max(2, min(args.steps, 10))
+    barrier()
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    if ws > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    if rank != 0:
+        if ws > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    peak = peak_fp64_tflops()
+    achieved = BATCH * FLOPS_PER / (ms * 1e-3) / 1e12
+    traffic = load_traffic()
+    value = ws * BATCH / (ms * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": "matrices/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded N(0,1), generated on device)",
+        "config": {"workload": WORKLOAD, "batch_per_gpu": BATCH, "n": N, "nrhs": NRHS,
+                   "parallelism": f"replicas x{ws}", "l2": "inputs 1.07 GB > L2, no flush"},
+        "gflops": value * FLOPS_PER / 1e9,
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak if peak else None,
+                     "traffic": traffic.get("bytes_per_launch") if traffic else None,
+                     "algorithmic_bytes": BATCH * BYTES_PER,
+                     "peak_source": "binary64 FMA probe kernel run in this process (MEASURED_PEAKS.json has no FP64 figure)",
+                     "kernel": "posv_thread_kernel"},
+        "e2e": {"value": ws * BATCH / (e2e_ms * 1e-3), "unit": "matrices/s",
+                "h2d_bytes_per_step": hA.numel() * 8 + hB.numel() * 8,
+                "d2h_bytes_per_step": hL.numel() * 8 + hX.numel() * 8},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+    }
+    hbm = None
+    try:
+        hbm = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs")
+    except (OSError, ValueError):
+        pass
+    gbs = BATCH * BYTES_PER / (ms * 1e-3) / 1e9
+    line["roofline_hbm"] = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                            "frac": gbs / hbm if hbm else None}
+    if ws == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline()
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,10 @@
+"""blast_gb300: batched GB300 (sm_103a) kernels for BLAST's small-matrix dense routines.
+
+The product is the C ABI library lib/libblastgpu.so (include/blastgpu.h). This package holds its
+build script, a ctypes binding, and ``blast``, a Python mirror of BLAST's function names over
+torch device tensors.
+"""
+from . import _lib
+from .blast import gemm, potrf, posv, potrs, col_major
+
+__all__ = ["gemm", "potrf", "posv", "potrs", "col_major", "_lib"]

@@ -1,0 +1,174 @@
+"""BLAST's hot-path API on batches of device matrices.
+
+Each function keeps the name, argument order and meaning of its BLAST counterpart (cited per
+function) and runs the sm_103a kernels of libblastgpu through the C ABI. A matrix is a float64
+CUDA tensor of shape (rows, cols) (one instance, BLAST's own call) or (batch, rows, cols)
+(a uniform batch). Storage is read from the strides:
+
+* column-major (stride(-2) == 1): BLAST's default dense storage, leading dimension stride(-1);
+* row-major (stride(-1) == 1): the storage of BLAST's ``trans()`` view of a column-major matrix,
+  so ``A.mT`` of a column-major tensor is BLAST's ``trans(A)``.
+
+Errors follow BLAST's: size mismatches raise ValueError (BLAST: std::invalid_argument "Matrix
+sizes do not match"), variants BLAST does not implement raise NotImplementedError (BLAST:
+std::logic_error). Calls are asynchronous on torch's current CUDA stream.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import torch
+
+from . import _lib
+
+COL, ROW, PANEL = 0, 1, 2
+
+
+@dataclass
+class _Mat:
+    ptr: int
+    rows: int
+    cols: int
+    ld: int
+    layout: int
+    batch: int
+    bstride: int
+
+
+def _stream() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _as_mat(t: torch.Tensor, name: str) -> _Mat:
+    if not isinstance(t, torch.Tensor):
+        raise TypeError(f"{name} must be a torch.Tensor")
+    if t.dtype != torch.float64:
+        raise TypeError(f"{name} must be float64 (BLAST's double), got {t.dtype}")
+    if not t.is_cuda:
+        raise ValueError(f"{name} must be a CUDA tensor")
+    if t.dim() == 2:
+        batch, bstride = 1, 0
+    elif t.dim() == 3:
+        batch, bstride = t.shape[0], t.stride(0)
+    else:
+        raise ValueError(f"{name} must have shape (rows, cols) or (batch, rows, cols)")
+    rows, cols = t.shape[-2], t.shape[-1]
+    s0, s1 = t.stride(-2), t.stride(-1)
+    if s0 == 1 and (s1 >= max(rows, 1) or cols <= 1):
+        layout, ld = COL, max(s1, rows, 1)
+    elif s1 == 1 and (s0 >= max(cols, 1) or rows <= 1):
+        layout, ld = ROW, max(s0, cols, 1)
+    else:
+        raise ValueError(f"{name} must be column-major or row-major per matrix (strides {t.stride()})")
+    return _Mat(t.data_ptr(), rows, cols, ld, layout, batch, bstride)
+
+
+def _batch_of(*mats: _Mat) -> int:
+    batches = {m.batch for m in mats}
+    if len(batches - {1}) > 1:
+        raise ValueError("Batch sizes do not match")
+    return max(batches)
+
+
+def _bstride(m: _Mat, batch: int) -> int:
+    return m.bstride if m.batch == batch else 0
+
+
+def gemm(*args):
+    """D = alpha*A*B + beta*C  (blast::gemm, algorithm/Gemm.hpp:80-97);
+    gemm(A, B, C, D) is D = A*B + C (algorithm/Gemm.hpp:113-118).
+
+    A and B may be column- or row-major (BLAST's trans() views); C and D are column-major.
+    """
+    if len(args) == 4:
+        alpha, (A, B, C, D), beta = 1.0, args, 1.0
+    elif len(args) == 6:
+        alpha, A, B, beta, C, D = args
+    else:
+        raise TypeError("gemm(alpha, A, B, beta, C, D) or gemm(A, B, C, D)")
+    a, b, c, d = (_as_mat(x, n) for x, n in ((A, "A"), (B, "B"), (C, "C"), (D, "D")))
+    M, N, K = a.rows, b.cols, a.cols
+    if b.rows != K or c.rows != M or c.cols != N or d.rows != M or d.cols != N:
+        raise ValueError("Matrix sizes do not match")
+    if c.layout != COL or d.layout != COL:
+        raise NotImplementedError("C and D must be column-major (BLAST's tile() requires it)")
+    batch = _batch_of(a, b, c, d)
+    if d.batch != batch:
+        raise ValueError("D must hold the whole batch")
+    _lib.call("blastgpu_dgemm_strided", int(a.layout == ROW), int(b.layout == ROW), M, N, K,
+              float(alpha), a.ptr, a.ld, _bstride(a, batch), b.ptr, b.ld, _bstride(b, batch),
+              float(beta), c.ptr, c.ld, _bstride(c, batch), d.ptr, d.ld, d.bstride, batch, _stream())
+    return D
+
+
+def _square_col(m: _Mat, name: str):
+    if m.layout != COL:
+        raise NotImplementedError(f"{name} must be column-major")
+
+
+def _info_tensor(batch: int, device) -> torch.Tensor:
+    return torch.empty(batch, dtype=torch.int32, device=device)
+
+
+def potrf(A: torch.Tensor, L: torch.Tensor) -> torch.Tensor:
+    """Lower Cholesky factor: L := chol(A)  (blast::potrf, dense/Potrf.hpp:66-106).
+
+    Reads the lower triangle of A; writes the lower triangle of L (L may be A). Returns the
+    per-instance info (0, or j+1 for the first non-positive pivot).
+    """
+    a, l = _as_mat(A, "A"), _as_mat(L, "L")
+    if a.cols > a.rows:
+        raise ValueError("Invalid matrix size")
+    if l.rows != a.rows or l.cols != a.cols:
+        raise ValueError("Invalid matrix size")
+    if a.rows != a.cols:
+        raise NotImplementedError("trapezoidal potrf (M > N) is not exposed by the batched ABI")
+    _square_col(a, "A")
+    _square_col(l, "L")
+    batch = _batch_of(a, l)
+    info = _info_tensor(batch, A.device)
+    _lib.call("blastgpu_dpotrf_strided", a.rows, a.ptr, a.ld, _bstride(a, batch), l.ptr, l.ld,
+              l.bstride, info.data_ptr(), batch, _stream())
+    return info
+
+
+def posv(A: torch.Tensor, L: torch.Tensor, B: torch.Tensor, X: torch.Tensor) -> torch.Tensor:
+    """Cholesky solve A*X = B: potrf(A, L), trsm<Lower>(L, B, X), trsm<Upper>(trans(L), X, X)
+    (dense/Potrf.hpp:66-106, dense/Trsm.hpp:17-66), fused in one launch. Returns info."""
+    a, l, b, x = (_as_mat(t, n) for t, n in ((A, "A"), (L, "L"), (B, "B"), (X, "X")))
+    n = a.rows
+    if a.cols != n or l.rows != n or l.cols != n or b.rows != n or x.rows != n or x.cols != b.cols:
+        raise ValueError("Invalid argument size")
+    for m, nm in ((a, "A"), (l, "L"), (b, "B"), (x, "X")):
+        _square_col(m, nm)
+    batch = _batch_of(a, l, b, x)
+    info = _info_tensor(batch, A.device)
+    _lib.call("blastgpu_dposv_strided", n, b.cols, a.ptr, a.ld, _bstride(a, batch), l.ptr, l.ld,
+              l.bstride, b.ptr, b.ld, _bstride(b, batch), x.ptr, x.ld, x.bstride, info.data_ptr(),
+              batch, _stream())
+    return info
+
+
+def potrs(L: torch.Tensor, B: torch.Tensor, X: torch.Tensor) -> torch.Tensor:
+    """X := A^{-1} B from the Cholesky factor L: trsm<Lower>(L, B, X) then
+    trsm<Upper>(trans(L), X, X) (dense/Trsm.hpp:17-66)."""
+    l, b, x = (_as_mat(t, n) for t, n in ((L, "L"), (B, "B"), (X, "X")))
+    n = l.rows
+    if l.cols != n or b.rows != n or x.rows != n or x.cols != b.cols:
+        raise ValueError("Invalid argument size")
+    for m, nm in ((l, "L"), (b, "B"), (x, "X")):
+        _square_col(m, nm)
+    batch = _batch_of(l, b, x)
+    _lib.call("blastgpu_dpotrs_strided", n, b.cols, l.ptr, l.ld, _bstride(l, batch), b.ptr, b.ld,
+              _bstride(b, batch), x.ptr, x.ld, x.bstride, batch, _stream())
+    return X
+
+
+def col_major(batch_shape, rows: int, cols: int, device="cuda", ld: int | None = None) -> torch.Tensor:
+    """An uninitialised column-major float64 tensor (…, rows, cols) with leading dimension ld."""
+    ld = rows if ld is None else ld
+    if ld < rows:
+        raise ValueError("ld < rows")
+    shape = tuple(batch_shape) + (cols, ld)
+    t = torch.empty(shape, dtype=torch.float64, device=device)
+    return t[..., :rows].transpose(-1, -2)

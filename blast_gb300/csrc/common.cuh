@@ -1,0 +1,100 @@
+// Shared device/host helpers of the blastgpu library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/blastgpu.h"
+
+namespace blastgpu {
+
+// Per-thread record of the last CUDA error, and a global launch counter.
+void set_cuda_error(cudaError_t e);
+void count_launch(int64_t n = 1);
+
+// Checks the launch that was just enqueued; returns a blastgpu status.
+inline int check_launch() {
+    cudaError_t const e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_cuda_error(e);
+        return BLASTGPU_ERR_CUDA;
+    }
+    count_launch();
+    return BLASTGPU_SUCCESS;
+}
+
+inline cudaStream_t as_cuda(blastgpu_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Number of SMs of the current device (cached per device).
+int sm_count();
+
+// ---------------------------------------------------------------------------------------------
+// Matrix views
+// ---------------------------------------------------------------------------------------------
+struct MatView {
+    double* p;
+    int32_t ld;
+    int32_t layout;
+    int32_t ps;
+
+    __device__ __forceinline__ int64_t off(int i, int j) const {
+        if (layout == BLASTGPU_COL_MAJOR) return i + (int64_t)j * ld;
+        if (layout == BLASTGPU_ROW_MAJOR) return (int64_t)i * ld + j;
+        return (int64_t)(i / ps) * ld + i % ps + (int64_t)j * ps;
+    }
+    __device__ __forceinline__ double& operator()(int i, int j) const { return p[off(i, j)]; }
+};
+
+__device__ __forceinline__ MatView view(blastgpu_mat const& m) {
+    return MatView{m.data, m.ld, m.layout, m.ps > 0 ? m.ps : 1};
+}
+
+// Host-side validation of one descriptor.
+inline bool mat_ok(blastgpu_mat const& m) {
+    if (m.rows < 0 || m.cols < 0 || m.reserved != 0) return false;
+    if (m.rows == 0 || m.cols == 0) return true;
+    if (!m.data) return false;
+    switch (m.layout) {
+        case BLASTGPU_COL_MAJOR: return m.ld >= m.rows;
+        case BLASTGPU_ROW_MAJOR: return m.ld >= m.cols;
+        case BLASTGPU_PANEL: return m.ps > 0 && m.ld >= (int64_t)m.ps * m.cols;
+        default: return false;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Reciprocal square root in binary64.
+// Newton-Raphson iteration for f(y) = 1/y^2 - s, y' = y*(3 - s*y^2)/2, seeded with the binary32
+// hardware estimate (about 23 correct bits); two steps give full binary64 accuracy (each step
+// roughly doubles the number of correct bits). Outside the binary32 normal range, and for
+// non-positive or NaN s, it falls back to the IEEE operations 1/sqrt(s).
+// The divisions and square roots this replaces cost about ten FMA issue slots each on GB300,
+// where the FP64 pipe is the bottleneck of every plain-FP64 kernel.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ double rsqrt_nr(double s) {
+    if (s > 1.0e-36 && s < 1.0e36) {
+        double y = (double)rsqrtf((float)s);
+        double const h = 0.5 * s;
+        y = y * fma(-h * y, y, 1.5);
+        y = y * fma(-h * y, y, 1.5);
+        return y;
+    }
+    return 1.0 / sqrt(s);
+}
+
+// Reciprocal by Newton-Raphson for f(y) = 1/y - a, y' = y*(2 - a*y), seeded with the binary32
+// estimate; same range fallback as rsqrt_nr.
+__device__ __forceinline__ double rcp_nr(double a) {
+    double const m = fabs(a);
+    if (m > 1.0e-36 && m < 1.0e36) {
+        double y = (double)__fdividef(1.0f, (float)a);
+        y = y * fma(-a, y, 2.0);
+        y = y * fma(-a, y, 2.0);
+        // One more correction with the residual e = 1 - a*y gives the last bits.
+        double const e = fma(-a, y, 1.0);
+        return fma(y, e, y);
+    }
+    return 1.0 / a;
+}
+
+}  // namespace blastgpu

@@ -1,0 +1,122 @@
+// Library-level entry points of blastgpu: version, status strings, error and launch accounting.
+#include <atomic>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+
+namespace blastgpu {
+
+namespace {
+thread_local int g_last_cuda_error = 0;
+std::atomic<int64_t> g_launches{0};
+}  // namespace
+
+void set_cuda_error(cudaError_t e) { g_last_cuda_error = static_cast<int>(e); }
+void count_launch(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+int sm_count() {
+    static std::mutex mu;
+    static std::vector<int> cache;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    std::lock_guard<std::mutex> lock(mu);
+    if ((int)cache.size() <= dev) cache.resize(dev + 1, 0);
+    if (cache[dev] == 0) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+        cache[dev] = n;
+    }
+    return cache[dev];
+}
+
+// Self-test kernels for the Newton-Raphson reciprocal helpers (compared against IEEE 1/sqrt(x)
+// and 1/x by the test-suite).
+__global__ void selftest_kernel(int which, const double* x, double* y, int n) {
+    int const i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = which == 0 ? rsqrt_nr(x[i]) : rcp_nr(x[i]);
+}
+
+// Binary64 FMA throughput probe: 8 independent FMA chains per thread; the result is consumed by
+// a comparison that never holds, so nothing is stored and nothing needs allocating.
+__global__ void fp64_probe_kernel(int iters, double a, double b, int* sink) {
+    double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+    double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; ++i) {
+        x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+        x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+    if (x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7 == -1.0) sink[0] = 1;
+}
+
+__device__ int g_probe_sink[1];
+
+}  // namespace blastgpu
+
+using namespace blastgpu;
+
+extern "C" {
+
+int blastgpu_version(void) { return 100; }
+
+const char* blastgpu_status_string(int status) {
+    switch (status) {
+        case BLASTGPU_SUCCESS: return "success";
+        case BLASTGPU_ERR_NOT_IMPLEMENTED: return "variant not implemented (BLAST throws std::logic_error)";
+        case BLASTGPU_ERR_CUDA: return "CUDA error";
+        case BLASTGPU_ERR_NO_DEVICE: return "no usable CUDA device";
+        case BLASTGPU_ERR_TOO_LARGE: return "size beyond the supported maximum";
+        default: break;
+    }
+    if (status < 0 && status > -100) return "invalid argument";
+    return "unknown status";
+}
+
+int blastgpu_last_cuda_error(void) { return g_last_cuda_error; }
+
+int64_t blastgpu_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+// Diagnostic export: y = rsqrt_nr(x) (which = 0) or rcp_nr(x) (which = 1), device arrays.
+int blastgpu_selftest_recip(int which, const double* x, double* y, int n, blastgpu_stream_t stream) {
+    if (which != 0 && which != 1) return -1;
+    if (n < 0) return -4;
+    if (n == 0) return BLASTGPU_SUCCESS;
+    if (!x) return -2;
+    if (!y) return -3;
+    selftest_kernel<<<(n + 255) / 256, 256, 0, as_cuda(stream)>>>(which, x, y, n);
+    return check_launch();
+}
+
+// Diagnostic export: measures the binary64 FMA throughput of the current device (TFLOP/s,
+// two flops per FMA) with CUDA events on `stream`; synchronises the stream.
+int blastgpu_probe_fp64_tflops(double* tflops, blastgpu_stream_t stream) {
+    if (!tflops) return -1;
+    cudaStream_t const s = as_cuda(stream);
+    int* sink = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void**>(&sink), g_probe_sink);
+    if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
+    int const threads = 256, blocks = sm_count() * 8, iters = 4096;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 0.f;
+    for (int rep = 0; rep < 3; ++rep) {
+        cudaEventRecord(e0, s);
+        fp64_probe_kernel<<<blocks, threads, 0, s>>>(iters, 0.999, 1e-3, sink);
+        cudaEventRecord(e1, s);
+        e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && (best == 0.f || ms < best)) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
+    *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+    return BLASTGPU_SUCCESS;
+}
+
+}  // extern "C"

@@ -1,0 +1,317 @@
+// Batched Cholesky factorisation and solve (potrf, potrs, posv), binary64, sm_103a.
+//
+// Reference: blast::potrf (dense/Potrf.hpp:20-106): left-looking, column strips of KN = 4,
+// each strip covered top-down by register tiles of 12, 8 and 4 rows (TileSize<double> = 4).
+// Per tile: load A, subtract L(i:,0:k)*L(k:k+4,0:k)^T with fused rank-1 updates (ger(-1,..)),
+// then either factor the diagonal tile in registers (RegisterMatrix::potrf,
+// register_matrix/RegisterMatrix.hpp:710-739) or solve against the diagonal block
+// (RegisterMatrix::trsm(Right, Upper), :566-602), and store.
+// The solves follow blast::trsm (dense/Trsm.hpp:17-66): L*Y = B, then trans(L)*X = Y.
+//
+// GPU mapping ("thread per matrix"): on GB300 the binary64 pipe issues one warp-wide FMA per
+// ~64 cycles per SM sub-partition (measured 1.2 TFLOP/s for the whole chip), and a division or
+// square root costs about ten FMA slots. Splitting one small factorisation over a warp leaves
+// most lanes idle on the diagonal (sqrt, reciprocal, short columns). Running BLAST's own
+// single-instance algorithm in every thread keeps all 32 lanes on useful FMAs, the diagonal
+// operations included, and keeps BLAST's register tiles (12/8/4 x 4) as the per-thread
+// accumulators. Each thread reads its own column segments, which stay in L1/L2 between the
+// strips of the left-looking sweep.
+//
+// Numerics: the per-element order of fused multiply-adds is BLAST's; the division by the pivot
+// (s / sqrt(s_cc), s / l_cc) becomes a multiplication by a reciprocal square root computed once
+// per column (rsqrt_nr). Results differ from BLAST's by a few units in the last place.
+#include "common.cuh"
+
+namespace blastgpu {
+namespace {
+
+constexpr int kThreads = 64;  // threads (= matrices) per CTA
+
+// One KM x 4 register tile of the left-looking strip k (rows i .. i+KM-1).
+template <int KM>
+__device__ __forceinline__ void potrf_tile(int n, int k, int i, int nc, const double* A, int lda,
+                                           double* L, int ldl, double (&y)[4], bool diag, int& info) {
+    double acc[KM][4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int r = 0; r < KM; ++r)
+            acc[r][c] = (c < nc && i + r < n) ? A[(i + r) + (int64_t)(k + c) * lda] : 0.0;
+
+    // acc -= L(i:i+KM, 0:k) * L(k:k+4, 0:k)^T, one fused rank-1 update per column l.
+    for (int l = 0; l < k; ++l) {
+        double const* Ll = L + (int64_t)l * ldl;
+        double a[KM], b[4];
+#pragma unroll
+        for (int r = 0; r < KM; ++r) a[r] = (i + r < n) ? Ll[i + r] : 0.0;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) b[c] = (c < nc) ? Ll[k + c] : 0.0;
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+#pragma unroll
+            for (int r = 0; r < KM; ++r) acc[r][c] = fma(-a[r], b[c], acc[r][c]);
+    }
+
+    if (diag) {
+        // In-register Cholesky of the strip (RegisterMatrix::potrf).
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            if (c < nc) {
+#pragma unroll
+                for (int j = 0; j < c; ++j) {
+                    double const lcj = acc[c][j];
+#pragma unroll
+                    for (int r = 0; r < KM; ++r) acc[r][c] = fma(-lcj, acc[r][j], acc[r][c]);
+                }
+                double const s = acc[c][c];
+                if (!(s > 0.0) && info == 0) info = k + c + 1;
+                y[c] = rsqrt_nr(s);
+#pragma unroll
+                for (int r = 0; r < KM; ++r) acc[r][c] *= y[c];
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+#pragma unroll
+            for (int r = 0; r < KM; ++r)
+                if (c < nc && r >= c && i + r < n) L[(i + r) + (int64_t)(k + c) * ldl] = acc[r][c];
+    } else {
+        // Right upper solve against the strip's diagonal block (RegisterMatrix::trsm).
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            if (c < nc) {
+#pragma unroll
+                for (int j = 0; j < c; ++j) {
+                    double const lcj = L[(k + c) + (int64_t)(k + j) * ldl];
+#pragma unroll
+                    for (int r = 0; r < KM; ++r) acc[r][c] = fma(-lcj, acc[r][j], acc[r][c]);
+                }
+#pragma unroll
+                for (int r = 0; r < KM; ++r) acc[r][c] *= y[c];
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+#pragma unroll
+            for (int r = 0; r < KM; ++r)
+                if (c < nc && i + r < n) L[(i + r) + (int64_t)(k + c) * ldl] = acc[r][c];
+    }
+}
+
+// Left-looking Cholesky of one n x n matrix; returns info (0 or first bad pivot + 1).
+__device__ int potrf_thread(int n, const double* A, int lda, double* L, int ldl) {
+    int info = 0;
+    for (int k = 0; k < n; k += 4) {
+        int const nc = min(4, n - k);
+        double y[4];
+        int i = k;
+        while (i < n) {
+            int const rem = n - i;
+            // BLAST's tile cover (dense/Potrf.hpp:97-104): 12 rows while more than 8 remain,
+            // then 8 while more than 4 remain, then 4.
+            if (rem > 8) { potrf_tile<12>(n, k, i, nc, A, lda, L, ldl, y, i == k, info); i += 12; }
+            else if (rem > 4) { potrf_tile<8>(n, k, i, nc, A, lda, L, ldl, y, i == k, info); i += 8; }
+            else { potrf_tile<4>(n, k, i, nc, A, lda, L, ldl, y, i == k, info); i += 4; }
+        }
+    }
+    return info;
+}
+
+constexpr int kRhs = 8;  // right-hand sides per register block of the solves
+
+// Forward solve L*Y = B (Y written to X; X may alias B), register blocks of 4 rows x kRhs.
+// Per element: acc = b_ij; for l < i ascending acc = fma(-l_il, y_lj, acc); y_ij = acc * (1/l_ii)
+// (dense/Trsm.hpp:39-52 with the division by l_ii as a multiplication by its reciprocal).
+__device__ void trsm_lower_thread(int n, int nrhs, const double* L, int ldl, const double* B, int ldb,
+                                  double* X, int ldx) {
+    for (int j0 = 0; j0 < nrhs; j0 += kRhs) {
+        int const nj = min(kRhs, nrhs - j0);
+        for (int i0 = 0; i0 < n; i0 += 4) {
+            int const ni = min(4, n - i0);
+            double acc[4][kRhs];
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int c = 0; c < kRhs; ++c)
+                    acc[r][c] = (r < ni && c < nj) ? B[(i0 + r) + (int64_t)(j0 + c) * ldb] : 0.0;
+            for (int l = 0; l < i0; ++l) {
+                double a[4], x[kRhs];
+#pragma unroll
+                for (int r = 0; r < 4; ++r) a[r] = (r < ni) ? L[(i0 + r) + (int64_t)l * ldl] : 0.0;
+#pragma unroll
+                for (int c = 0; c < kRhs; ++c) x[c] = (c < nj) ? X[l + (int64_t)(j0 + c) * ldx] : 0.0;
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+#pragma unroll
+                    for (int c = 0; c < kRhs; ++c) acc[r][c] = fma(-a[r], x[c], acc[r][c]);
+            }
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                if (r < ni) {
+#pragma unroll
+                    for (int q = 0; q < r; ++q) {
+                        double const lrq = L[(i0 + r) + (int64_t)(i0 + q) * ldl];
+#pragma unroll
+                        for (int c = 0; c < kRhs; ++c) acc[r][c] = fma(-lrq, acc[q][c], acc[r][c]);
+                    }
+                    double const d = rcp_nr(L[(i0 + r) + (int64_t)(i0 + r) * ldl]);
+#pragma unroll
+                    for (int c = 0; c < kRhs; ++c) acc[r][c] *= d;
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int c = 0; c < kRhs; ++c)
+                    if (r < ni && c < nj) X[(i0 + r) + (int64_t)(j0 + c) * ldx] = acc[r][c];
+        }
+    }
+}
+
+// Backward solve L^T*X = Y in place in X (trsm<Upper> on trans(L), dense/Trsm.hpp:53-65).
+__device__ void trsm_lower_trans_thread(int n, int nrhs, const double* L, int ldl, double* X, int ldx) {
+    int const last = ((n - 1) / 4) * 4;
+    for (int j0 = 0; j0 < nrhs; j0 += kRhs) {
+        int const nj = min(kRhs, nrhs - j0);
+        for (int i0 = last; i0 >= 0; i0 -= 4) {
+            int const ni = min(4, n - i0);
+            double acc[4][kRhs];
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int c = 0; c < kRhs; ++c)
+                    acc[r][c] = (r < ni && c < nj) ? X[(i0 + r) + (int64_t)(j0 + c) * ldx] : 0.0;
+            for (int l = i0 + 4; l < n; ++l) {
+                double a[4], x[kRhs];
+#pragma unroll
+                for (int r = 0; r < 4; ++r) a[r] = (r < ni) ? L[l + (int64_t)(i0 + r) * ldl] : 0.0;
+#pragma unroll
+                for (int c = 0; c < kRhs; ++c) x[c] = (c < nj) ? X[l + (int64_t)(j0 + c) * ldx] : 0.0;
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+#pragma unroll
+                    for (int c = 0; c < kRhs; ++c) acc[r][c] = fma(-a[r], x[c], acc[r][c]);
+            }
+#pragma unroll
+            for (int r = 3; r >= 0; --r) {
+                if (r < ni) {
+#pragma unroll
+                    for (int q = r + 1; q < 4; ++q) {
+                        if (q < ni) {
+                            double const lqr = L[(i0 + q) + (int64_t)(i0 + r) * ldl];
+#pragma unroll
+                            for (int c = 0; c < kRhs; ++c) acc[r][c] = fma(-lqr, acc[q][c], acc[r][c]);
+                        }
+                    }
+                    double const d = rcp_nr(L[(i0 + r) + (int64_t)(i0 + r) * ldl]);
+#pragma unroll
+                    for (int c = 0; c < kRhs; ++c) acc[r][c] *= d;
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int c = 0; c < kRhs; ++c)
+                    if (r < ni && c < nj) X[(i0 + r) + (int64_t)(j0 + c) * ldx] = acc[r][c];
+        }
+    }
+}
+
+struct PosvArgs {
+    int n, nrhs;
+    const double* A; int lda; int64_t sa;
+    double* L; int ldl; int64_t sl;
+    const double* B; int ldb; int64_t sb;
+    double* X; int ldx; int64_t sx;
+    int32_t* info;
+    int64_t batch;
+    int mode;  // 0 potrf, 1 potrf + solves, 2 solves only
+};
+
+__global__ void __launch_bounds__(kThreads) posv_thread_kernel(PosvArgs p) {
+    int64_t const b = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+    if (b >= p.batch) return;
+    double* L = p.L + b * p.sl;
+    int info = 0;
+    if (p.mode != 2) {
+        info = potrf_thread(p.n, p.A + b * p.sa, p.lda, L, p.ldl);
+        if (p.info) p.info[b] = info;
+    }
+    if (p.mode != 0 && p.nrhs > 0) {
+        double* X = p.X + b * p.sx;
+        trsm_lower_thread(p.n, p.nrhs, L, p.ldl, p.B + b * p.sb, p.ldb, X, p.ldx);
+        trsm_lower_trans_thread(p.n, p.nrhs, L, p.ldl, X, p.ldx);
+    }
+}
+
+int launch_posv(PosvArgs const& p, cudaStream_t stream) {
+    if (p.batch == 0 || p.n == 0) {
+        if (p.info && p.batch > 0) {
+            cudaError_t const e = cudaMemsetAsync(p.info, 0, sizeof(int32_t) * p.batch, stream);
+            if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
+        }
+        return BLASTGPU_SUCCESS;
+    }
+    int64_t const blocks = (p.batch + kThreads - 1) / kThreads;
+    if (blocks > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
+    posv_thread_kernel<<<(unsigned)blocks, kThreads, 0, stream>>>(p);
+    return check_launch();
+}
+
+}  // namespace
+}  // namespace blastgpu
+
+using namespace blastgpu;
+
+extern "C" {
+
+int blastgpu_dpotrf_strided(int n, const double* A, int lda, int64_t stride_a, double* L, int ldl,
+                            int64_t stride_l, int32_t* info, int64_t batch, blastgpu_stream_t stream) {
+    if (n < 0) return -1;
+    if (n > 0 && !A) return -2;
+    if (lda < (n > 0 ? n : 1)) return -3;
+    if (n > 0 && !L) return -5;
+    if (ldl < (n > 0 ? n : 1)) return -6;
+    if (batch < 0) return -9;
+    PosvArgs p{n, 0, A, lda, stride_a, L, ldl, stride_l, nullptr, 1, 0, nullptr, 1, 0, info, batch, 0};
+    return launch_posv(p, as_cuda(stream));
+}
+
+int blastgpu_dposv_strided(int n, int nrhs, const double* A, int lda, int64_t stride_a, double* L,
+                           int ldl, int64_t stride_l, const double* B, int ldb, int64_t stride_b,
+                           double* X, int ldx, int64_t stride_x, int32_t* info, int64_t batch,
+                           blastgpu_stream_t stream) {
+    if (n < 0) return -1;
+    if (nrhs < 0) return -2;
+    if (n > 0 && !A) return -3;
+    if (lda < (n > 0 ? n : 1)) return -4;
+    if (n > 0 && !L) return -6;
+    if (ldl < (n > 0 ? n : 1)) return -7;
+    if (n > 0 && nrhs > 0 && !B) return -9;
+    if (ldb < (n > 0 ? n : 1)) return -10;
+    if (n > 0 && nrhs > 0 && !X) return -12;
+    if (ldx < (n > 0 ? n : 1)) return -13;
+    if (batch < 0) return -16;
+    PosvArgs p{n, nrhs, A, lda, stride_a, L, ldl, stride_l, B, ldb, stride_b, X, ldx, stride_x, info, batch, 1};
+    return launch_posv(p, as_cuda(stream));
+}
+
+int blastgpu_dpotrs_strided(int n, int nrhs, const double* L, int ldl, int64_t stride_l,
+                            const double* B, int ldb, int64_t stride_b, double* X, int ldx,
+                            int64_t stride_x, int64_t batch, blastgpu_stream_t stream) {
+    if (n < 0) return -1;
+    if (nrhs < 0) return -2;
+    if (n > 0 && !L) return -3;
+    if (ldl < (n > 0 ? n : 1)) return -4;
+    if (n > 0 && nrhs > 0 && !B) return -6;
+    if (ldb < (n > 0 ? n : 1)) return -7;
+    if (n > 0 && nrhs > 0 && !X) return -9;
+    if (ldx < (n > 0 ? n : 1)) return -10;
+    if (batch < 0) return -12;
+    if (nrhs == 0) return BLASTGPU_SUCCESS;
+    PosvArgs p{n, nrhs, nullptr, 1, 0, const_cast<double*>(L), ldl, stride_l, B, ldb, stride_b, X, ldx,
+               stride_x, nullptr, batch, 2};
+    return launch_posv(p, as_cuda(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,142 @@
+/*
+ * blastgpu.h - C ABI of the batched GB300 (sm_103a) implementation of BLAST's small-matrix
+ * dense kernels (mkatliar/blast, "BLAS Templates").
+ *
+ * BLAST is a header-only C++ template library: every routine works on ONE matrix in the
+ * caller's thread, and reports errors by throwing. This ABI replaces those call sites with
+ * batched, stream-ordered entry points:
+ *
+ *   - plain pointers and sizes only (no C++ or torch types), callable from C, C++ (see
+ *     blastgpu/blast.hpp for a shim with BLAST's own function names), Python ctypes, etc.;
+ *   - every pointer to matrix data is a DEVICE pointer (the library never copies host data);
+ *   - a batch of one instance is the drop-in for one BLAST call; a "strided" entry point takes
+ *     a uniform batch (instance b at base + b*stride), a "batched" entry point takes an array of
+ *     per-instance descriptors in device memory (ragged batches: every instance its own sizes);
+ *   - every call is asynchronous on the given stream, allocates nothing and never synchronises;
+ *   - the return value is a status (0 = success; a negative value -i means argument i, counted
+ *     from 1, is invalid, LAPACK style; see blastgpu_status); numerical failures are reported per
+ *     instance in an `info` array (LAPACK convention) instead of BLAST's exceptions.
+ *
+ * Element (i, j) of a blastgpu_mat lives at
+ *   BLASTGPU_COL_MAJOR  data[i + j*ld]                         (dense/StaticMatrix.hpp:152-165)
+ *   BLASTGPU_ROW_MAJOR  data[i*ld + j]                         (BLAST's trans() views)
+ *   BLASTGPU_PANEL      data[(i/ps)*ld + i%ps + j*ps]          (panel/StaticPanelMatrix.hpp:178-184)
+ * with ld >= rows (col), >= cols (row), >= ps*cols (panel; BLAST calls it the panel "spacing").
+ *
+ * All floating-point work is IEEE binary64. Results agree with BLAST's algorithm run on the same
+ * inputs to a normwise relative error <= 10*n*eps (most kernels reproduce BLAST's order of fused
+ * multiply-adds exactly; divisions by a pivot are done as multiplications by its reciprocal).
+ */
+#ifndef BLASTGPU_H
+#define BLASTGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Opaque CUDA stream handle (identical to cudaStream_t / CUstream). NULL = legacy default stream. */
+typedef struct CUstream_st* blastgpu_stream_t;
+
+typedef enum blastgpu_status {
+    BLASTGPU_SUCCESS = 0,
+    /* -1 ... -99: -(index of the first invalid argument) */
+    BLASTGPU_ERR_NOT_IMPLEMENTED = -1001, /* variant BLAST itself rejects with std::logic_error */
+    BLASTGPU_ERR_CUDA = -1002,            /* a CUDA launch/runtime error; see blastgpu_last_cuda_error() */
+    BLASTGPU_ERR_NO_DEVICE = -1003,       /* no usable sm_103 device */
+    BLASTGPU_ERR_TOO_LARGE = -1004        /* a size beyond what the selected kernel supports */
+} blastgpu_status;
+
+typedef enum blastgpu_layout {
+    BLASTGPU_COL_MAJOR = 0,
+    BLASTGPU_ROW_MAJOR = 1,
+    BLASTGPU_PANEL = 2
+} blastgpu_layout;
+
+typedef enum blastgpu_uplo { BLASTGPU_LOWER = 0, BLASTGPU_UPPER = 1 } blastgpu_uplo;
+typedef enum blastgpu_side { BLASTGPU_LEFT = 0, BLASTGPU_RIGHT = 1 } blastgpu_side;
+
+/* One matrix (or a view of one): BLAST's MatrixPointer + its extents. 32 bytes. */
+typedef struct blastgpu_mat {
+    double* data;     /* device pointer to element (0, 0) */
+    int32_t rows;
+    int32_t cols;
+    int32_t ld;       /* leading dimension / panel spacing, in elements */
+    int32_t layout;   /* blastgpu_layout */
+    int32_t ps;       /* panel height for BLASTGPU_PANEL (BLAST: SIMD width, 4 on AVX2, 2 on NEON) */
+    int32_t reserved; /* must be 0 */
+} blastgpu_mat;
+
+/* ---------------------------------------------------------------------------------------------
+ * Library information
+ * ------------------------------------------------------------------------------------------- */
+int blastgpu_version(void);                /* 10000*major + 100*minor + patch */
+const char* blastgpu_status_string(int status);
+int blastgpu_last_cuda_error(void);        /* cudaError_t of the last BLASTGPU_ERR_CUDA (per thread) */
+/* Number of kernels this library has launched since load (all threads); for launch accounting. */
+int64_t blastgpu_launch_count(void);
+
+/* Diagnostics (no BLAST counterpart). selftest_recip: y[i] = 1/sqrt(x[i]) (which = 0) or 1/x[i]
+ * (which = 1) with the library's Newton-Raphson helpers, device arrays. probe_fp64_tflops:
+ * measures the device's binary64 FMA throughput (TFLOP/s) on `stream` and synchronises it. */
+int blastgpu_selftest_recip(int which, const double* x, double* y, int n, blastgpu_stream_t stream);
+int blastgpu_probe_fp64_tflops(double* tflops, blastgpu_stream_t stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * gemm: D = alpha*A*B + beta*C
+ * Replaces blast::gemm(alpha, A, B, beta, C, D)        (algorithm/Gemm.hpp:80-97),
+ *          blast::gemm(A, B, C, D)                     (algorithm/Gemm.hpp:113-118, alpha=beta=1),
+ *          blast::gemm(M, N, K, alpha, pA, pB, beta, pC, pD) (algorithm/Gemm.hpp:41-62).
+ * trans_a/trans_b = 1 take A / B as row-major storage (BLAST's trans() view of a column-major
+ * matrix).  C may equal D (in place, as getrf's trailing update does, dense/Getrf.hpp:91-101).
+ * Per element: acc = sum_k fma(a_ik, b_kj, acc) in ascending k; d = fma(beta, c, alpha*acc).
+ * ------------------------------------------------------------------------------------------- */
+int blastgpu_dgemm_strided(int trans_a, int trans_b, int m, int n, int k, double alpha,
+                           const double* A, int lda, int64_t stride_a,
+                           const double* B, int ldb, int64_t stride_b, double beta,
+                           const double* C, int ldc, int64_t stride_c,
+                           double* D, int ldd, int64_t stride_d,
+                           int64_t batch, blastgpu_stream_t stream);
+
+typedef struct blastgpu_gemm_desc {
+    blastgpu_mat A, B, C, D;
+    double alpha, beta;
+} blastgpu_gemm_desc; /* 144 bytes */
+
+/* desc: device array of `batch` descriptors; max_m/max_n/max_k bound every instance's sizes
+ * (they select the kernel shape; instances may be smaller). */
+int blastgpu_dgemm_batched(const blastgpu_gemm_desc* desc, int64_t batch, int max_m, int max_n,
+                           int max_k, blastgpu_stream_t stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * potrf: lower Cholesky factor L of a symmetric positive definite n x n A (only the lower
+ * triangle of A is read; the strict upper triangle of L is not written). L may equal A.
+ * Replaces blast::potrf(A, L) dense (dense/Potrf.hpp:66-106) and panel (panel/Potrf.hpp:59-106).
+ * info[b] = 0, or j+1 if the j-th pivot was not positive (BLAST does not check and returns NaNs;
+ * the factor is computed the same way and carries the same NaNs). info may be NULL.
+ * ------------------------------------------------------------------------------------------- */
+int blastgpu_dpotrf_strided(int n, const double* A, int lda, int64_t stride_a,
+                            double* L, int ldl, int64_t stride_l, int32_t* info,
+                            int64_t batch, blastgpu_stream_t stream);
+
+/* potrf followed by the two triangular solves L*Y = B, L^T*X = Y (BLAST has no potrs; this is
+ * potrf + trsm<Lower> + trsm<Upper> on trans(L), dense/Trsm.hpp:17-66), fused in one kernel.
+ * B is n x nrhs; X may equal B; L may equal A. */
+int blastgpu_dposv_strided(int n, int nrhs, const double* A, int lda, int64_t stride_a,
+                           double* L, int ldl, int64_t stride_l,
+                           const double* B, int ldb, int64_t stride_b,
+                           double* X, int ldx, int64_t stride_x, int32_t* info,
+                           int64_t batch, blastgpu_stream_t stream);
+
+/* The two triangular solves alone, given the factor L from potrf. X may equal B. */
+int blastgpu_dpotrs_strided(int n, int nrhs, const double* L, int ldl, int64_t stride_l,
+                            const double* B, int ldb, int64_t stride_b,
+                            double* X, int ldx, int64_t stride_x,
+                            int64_t batch, blastgpu_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BLASTGPU_H */
