@@ -195,6 +195,7 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=dev)
     stream = torch.cuda.current_stream()
 
+    BATCH = args.batch
     A, B = make_inputs(BATCH, 1234 + rank, dev)
     L = bg.col_major((BATCH,), N, N, dev)
     X = bg.col_major((BATCH,), N, NRHS, dev)
@@ -228,6 +229,10 @@ def run_ours(args):
         t = torch.tensor([ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
+
+    if args.no_e2e:
+        print(json.dumps({"ms_per_step": ms, "value": ws * BATCH / (ms * 1e-3), "batch": BATCH}))
+        return
 
     # End to end through the public API: pinned host A, B -> device -> posv -> L, X to host.
     hA = torch.empty(A.mT.shape, dtype=torch.float64, pin_memory=True)
@@ -308,10 +313,13 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true",
+                    help="device-timed leg only (small profiling runs); prints a reduced line")
+    ap.add_argument("--batch", type=int, default=BATCH, help="matrices per GPU (default 50,000)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

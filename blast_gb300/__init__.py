@@ -5,6 +5,6 @@ build script, a ctypes binding, and ``blast``, a Python mirror of BLAST's functi
 torch device tensors.
 """
 from . import _lib
-from .blast import gemm, potrf, posv, potrs, col_major
+from .blast import col_major, gemm, getrf, getrs, posv, potrf, potrs
 
-__all__ = ["gemm", "potrf", "posv", "potrs", "col_major", "_lib"]
+__all__ = ["gemm", "potrf", "posv", "potrs", "getrf", "getrs", "col_major", "_lib"]

@@ -46,6 +46,8 @@ SIGNATURES: dict[str, list] = {
     "blastgpu_launch_count": [],
     "blastgpu_selftest_recip": [I32, PTR, PTR, I32, PTR],
     "blastgpu_probe_fp64_tflops": [PTR, PTR],
+    "blastgpu_tune_set": [C.c_char_p, I32],
+    "blastgpu_tune_get": [C.c_char_p, PTR],
     "blastgpu_dgemm_strided": [I32, I32, I32, I32, I32, DBL, PTR, I32, I64, PTR, I32, I64, DBL,
                                PTR, I32, I64, PTR, I32, I64, I64, PTR],
     "blastgpu_dgemm_batched": [PTR, I64, I32, I32, I32, PTR],
@@ -53,6 +55,11 @@ SIGNATURES: dict[str, list] = {
     "blastgpu_dposv_strided": [I32, I32, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, PTR, I32,
                                I64, PTR, I64, PTR],
     "blastgpu_dpotrs_strided": [I32, I32, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, I64, PTR],
+    "blastgpu_dgetrf_strided": [I32, I32, PTR, I32, I64, PTR, I64, PTR, I64, PTR],
+    "blastgpu_dgetrs_strided": [I32, I32, PTR, I32, I64, PTR, I64, PTR, I32, I64, PTR, I64, PTR],
+    "blastgpu_dgetrf_batched": [PTR, PTR, I64, PTR],
+    "blastgpu_dgetrs_batched": [PTR, PTR, I64, PTR],
+    "blastgpu_dgesv_batched": [PTR, PTR, I64, PTR],
 }
 _RESTYPES = {"blastgpu_status_string": C.c_char_p, "blastgpu_launch_count": C.c_int64}
 
@@ -87,6 +94,16 @@ def call(name: str, *args) -> int:
             detail += f", cudaError {lib().blastgpu_last_cuda_error()}"
         raise BlastGpuError(name, st, detail)
     return st
+
+
+def tune_set(key: str, value: int) -> None:
+    call("blastgpu_tune_set", key.encode(), int(value))
+
+
+def tune_get(key: str):
+    v = C.c_int(0)
+    st = lib().blastgpu_tune_get(key.encode(), C.byref(v))
+    return v.value if st == 0 else None
 
 
 def launch_count() -> int:

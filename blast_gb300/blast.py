@@ -164,6 +164,51 @@ def potrs(L: torch.Tensor, B: torch.Tensor, X: torch.Tensor) -> torch.Tensor:
     return X
 
 
+def _ipiv_check(ipiv: torch.Tensor, batch: int, k: int, name="ipiv"):
+    if ipiv.dtype != torch.int32 or not ipiv.is_cuda:
+        raise TypeError(f"{name} must be an int32 CUDA tensor")
+    want = (k,) if batch == 1 and ipiv.dim() == 1 else (batch, k)
+    if tuple(ipiv.shape) != want or ipiv.stride(-1) != 1:
+        raise ValueError(f"{name} must have shape {want} and unit stride")
+
+
+def getrf(A: torch.Tensor, ipiv: torch.Tensor) -> torch.Tensor:
+    """LU with partial pivoting in place: A = P*L*U (blast::getrf, dense/Getrf.hpp:52-119).
+
+    A: column-major (…, m, n); ipiv: int32 (…, min(m, n)) receiving 0-based pivot rows.
+    Returns info (0, or k+1 for the first exactly-zero pivot; BLAST throws "Matrix is singular").
+    """
+    a = _as_mat(A, "A")
+    if a.layout != COL:
+        raise NotImplementedError("getrf needs column-major storage (BLAST's row-major overload "
+                                  "does not pivot)")
+    k = min(a.rows, a.cols)
+    _ipiv_check(ipiv, a.batch, k)
+    info = _info_tensor(a.batch, A.device)
+    sp = ipiv.stride(0) if ipiv.dim() == 2 else 0
+    _lib.call("blastgpu_dgetrf_strided", a.rows, a.cols, a.ptr, a.ld, a.bstride, ipiv.data_ptr(),
+              sp, info.data_ptr(), a.batch, _stream())
+    return info
+
+
+def getrs(LU: torch.Tensor, ipiv: torch.Tensor, X: torch.Tensor, info: torch.Tensor | None = None):
+    """X := A^{-1} X from getrf's factors: laswp, trsm<Lower, unit>, trsm<Upper>
+    (dense/Laswp.hpp:37-43, dense/Trsm.hpp:17-66). Instances with info != 0 are skipped."""
+    lu, x = _as_mat(LU, "LU"), _as_mat(X, "X")
+    n = lu.rows
+    if lu.cols != n or x.rows != n:
+        raise ValueError("Invalid argument size")
+    _square_col(lu, "LU")
+    _square_col(x, "X")
+    batch = _batch_of(lu, x)
+    _ipiv_check(ipiv, lu.batch, n)
+    sp = ipiv.stride(0) if ipiv.dim() == 2 else 0
+    _lib.call("blastgpu_dgetrs_strided", n, x.cols, lu.ptr, lu.ld, _bstride(lu, batch),
+              ipiv.data_ptr(), sp, x.ptr, x.ld, x.bstride,
+              info.data_ptr() if info is not None else None, batch, _stream())
+    return X
+
+
 def col_major(batch_shape, rows: int, cols: int, device="cuda", ld: int | None = None) -> torch.Tensor:
     """An uninitialised column-major float64 tensor (…, rows, cols) with leading dimension ld."""
     ld = rows if ld is None else ld

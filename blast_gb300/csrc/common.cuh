@@ -28,6 +28,9 @@ inline cudaStream_t as_cuda(blastgpu_stream_t s) { return reinterpret_cast<cudaS
 // Number of SMs of the current device (cached per device).
 int sm_count();
 
+// Kernel-selection parameters set by the autotuner (blastgpu_tune_set); `fallback` if unset.
+int tune_get(const char* key, int fallback);
+
 // ---------------------------------------------------------------------------------------------
 // Matrix views
 // ---------------------------------------------------------------------------------------------

@@ -1,6 +1,9 @@
 // Library-level entry points of blastgpu: version, status strings, error and launch accounting.
 #include <atomic>
+#include <cstring>
+#include <map>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "common.cuh"
@@ -14,6 +17,21 @@ std::atomic<int64_t> g_launches{0};
 
 void set_cuda_error(cudaError_t e) { g_last_cuda_error = static_cast<int>(e); }
 void count_launch(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+namespace {
+std::mutex g_tune_mu;
+std::map<std::string, int>& tune_table() {
+    static std::map<std::string, int> t;
+    return t;
+}
+}  // namespace
+
+int tune_get(const char* key, int fallback) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto const& t = tune_table();
+    auto it = t.find(key);
+    return it == t.end() ? fallback : it->second;
+}
 
 int sm_count() {
     static std::mutex mu;
@@ -37,19 +55,19 @@ __global__ void selftest_kernel(int which, const double* x, double* y, int n) {
     if (i < n) y[i] = which == 0 ? rsqrt_nr(x[i]) : rcp_nr(x[i]);
 }
 
-// Binary64 FMA throughput probe: 8 independent FMA chains per thread; the result is consumed by
-// a comparison that never holds, so nothing is stored and nothing needs allocating.
-__global__ void fp64_probe_kernel(int iters, double a, double b, int* sink) {
+// Binary64 FMA throughput probe: 8 independent FMA chains per thread; every CTA stores its
+// per-thread sums into one small static array, so nothing needs allocating.
+__global__ void fp64_probe_kernel(int iters, double a, double b, double* sink) {
     double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
     double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
     for (int i = 0; i < iters; ++i) {
         x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
         x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
     }
-    if (x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7 == -1.0) sink[0] = 1;
+    sink[threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
-__device__ int g_probe_sink[1];
+__device__ double g_probe_sink[256];
 
 }  // namespace blastgpu
 
@@ -74,6 +92,24 @@ const char* blastgpu_status_string(int status) {
 
 int blastgpu_last_cuda_error(void) { return g_last_cuda_error; }
 
+int blastgpu_tune_set(const char* key, int value) {
+    if (!key || !*key || std::strlen(key) > 64) return -1;
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    tune_table()[key] = value;
+    return BLASTGPU_SUCCESS;
+}
+
+int blastgpu_tune_get(const char* key, int* value) {
+    if (!key || !*key) return -1;
+    if (!value) return -2;
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto const& t = tune_table();
+    auto it = t.find(key);
+    if (it == t.end()) return -1;
+    *value = it->second;
+    return BLASTGPU_SUCCESS;
+}
+
 int64_t blastgpu_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 // Diagnostic export: y = rsqrt_nr(x) (which = 0) or rcp_nr(x) (which = 1), device arrays.
@@ -92,7 +128,7 @@ int blastgpu_selftest_recip(int which, const double* x, double* y, int n, blastg
 int blastgpu_probe_fp64_tflops(double* tflops, blastgpu_stream_t stream) {
     if (!tflops) return -1;
     cudaStream_t const s = as_cuda(stream);
-    int* sink = nullptr;
+    double* sink = nullptr;
     cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void**>(&sink), g_probe_sink);
     if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
     int const threads = 256, blocks = sm_count() * 8, iters = 4096;

@@ -1,0 +1,332 @@
+// Batched LU with partial pivoting (getrf), row interchanges (laswp) and the LU solve (getrs),
+// binary64, sm_103a.
+//
+// Reference: blast::getrf (dense/Getrf.hpp:52-119), right-looking with NB = TileSize<double> = 4:
+//   getf2 on the (M-k) x 4 panel (dense/Getf2.hpp:52-77: iamax pivot, swap within the panel,
+//   singular check, scale by the pivot, rank-1 update), pivot adjustment, laswp of the other
+//   columns (dense/Laswp.hpp:37-43), U12 := L11^{-1} A12 (trsm<Lower, unit>, dense/Trsm.hpp),
+//   A22 := A22 - A21*U12 through gemm (K = 4: acc = sum of fused products from 0, d = c - acc);
+//   unblocked getf2 on the remainder; laswp of the left columns.
+// BLAST has no getrs: it is laswp(b), trsm<Lower, unit>, trsm<Upper> (scalar loops, dense/Trsm.hpp).
+//
+// GPU mapping:
+//  * getrf: one warp per matrix, the matrix in global memory (L1/L2 resident while its warp works
+//    on it). Lanes split every step: the pivot search is a warp-shuffle argmax that keeps the
+//    first maximum (BLAST's strict '>' scan, dense/Iamax.hpp:82-95), swaps and laswp go lane per
+//    column, scaling and rank-1 updates lane per row, the trailing update lane per element.
+//    Every element sees exactly BLAST's sequence of rounded operations (the pivot scaling is an
+//    IEEE division, as in BLAST), so factors and pivot sequences are bit-identical to the oracle.
+//  * getrs: one thread per matrix. The backward substitution is a chain of dependent dot
+//    products in BLAST's order (each x_i starts from x_{i+1}); running whole solves per thread
+//    keeps every lane busy while preserving that order.
+#include "common.cuh"
+
+namespace blastgpu {
+namespace {
+
+constexpr int kWarps = 4;  // matrices (warps) per CTA of the getrf kernel
+
+struct GetrfItem {
+    double* a;
+    int m, n, lda;
+    int32_t* ipiv;
+};
+
+struct StridedGetrf {
+    int m, n, lda;
+    double* A;
+    int64_t sa;
+    int32_t* ipiv;
+    int64_t sp;
+    __device__ GetrfItem get(int64_t b) const { return {A + b * sa, m, n, lda, ipiv + b * sp}; }
+};
+
+struct DescGetrf {
+    const blastgpu_getrf_desc* desc;
+    __device__ GetrfItem get(int64_t b) const {
+        blastgpu_getrf_desc const& d = desc[b];
+        return {d.A.data, d.A.rows, d.A.cols, d.A.ld, d.ipiv};
+    }
+};
+
+// First index of the largest |x|, rows [r0, r1) of column j, as BLAST's scalar scan would find:
+// a value replaces the running maximum only if strictly larger, so the first maximum wins and
+// NaN never wins unless it is the first element (then nothing replaces it).
+__device__ __forceinline__ int warp_iamax(const double* a, int lda, int r0, int r1, int j, int lane) {
+    double best = -1.0;
+    int idx = 0x7fffffff;
+    for (int r = r0 + lane; r < r1; r += 32) {
+        double const v = fabs(a[r + (int64_t)j * lda]);
+        if (v > best) { best = v; idx = r; }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        double const ob = __shfl_xor_sync(0xffffffffu, best, off);
+        int const oi = __shfl_xor_sync(0xffffffffu, idx, off);
+        if (ob > best || (ob == best && oi < idx)) { best = ob; idx = oi; }
+    }
+    double const first = a[r0 + (int64_t)j * lda];
+    if (first != first || idx == 0x7fffffff) idx = r0;  // NaN first element, or all NaN
+    return idx - r0;
+}
+
+// getf2 (dense/Getf2.hpp:52-77) on the m x n block at (r0, c0); swaps cover the block's columns.
+// ipiv receives block-relative pivots. Returns the block-relative k+1 of a zero pivot, or 0.
+__device__ int warp_getf2(double* a, int lda, int r0, int c0, int m, int n, int32_t* ipiv, int lane) {
+    for (int k = 0; k < m && k < n; ++k) {
+        int const ip = warp_iamax(a, lda, r0 + k, r0 + m, c0 + k, lane) + k;
+        if (lane == 0) ipiv[k] = ip;
+        if (ip != k) {
+            for (int j = lane; j < n; j += 32) {
+                double* p = a + (int64_t)(c0 + j) * lda;
+                double const t = p[r0 + k];
+                p[r0 + k] = p[r0 + ip];
+                p[r0 + ip] = t;
+            }
+        }
+        __syncwarp();
+        double const piv = a[(r0 + k) + (int64_t)(c0 + k) * lda];
+        if (piv == 0.0) return k + 1;
+        double* col = a + (int64_t)(c0 + k) * lda;
+        for (int i = k + 1 + lane; i < m; i += 32) col[r0 + i] = col[r0 + i] / piv;
+        __syncwarp();
+        for (int j = k + 1; j < n; ++j) {
+            double* cj = a + (int64_t)(c0 + j) * lda;
+            double const y = cj[r0 + k];
+            for (int i = k + 1 + lane; i < m; i += 32) cj[r0 + i] = fma(-col[r0 + i], y, cj[r0 + i]);
+        }
+        __syncwarp();
+    }
+    return 0;
+}
+
+// laswp on columns [c0, c1) with pivots ipiv[k0..k1) (dense/Laswp.hpp:37-43), lane per column.
+__device__ __forceinline__ void warp_laswp(double* a, int lda, int c0, int c1, int k0, int k1,
+                                           const int32_t* ipiv, int lane) {
+    for (int j = c0 + lane; j < c1; j += 32) {
+        double* p = a + (int64_t)j * lda;
+        for (int k = k0; k < k1; ++k) {
+            int const q = ipiv[k];
+            if (q != k) {
+                double const t = p[k];
+                p[k] = p[q];
+                p[q] = t;
+            }
+        }
+    }
+}
+
+__device__ int warp_getrf(GetrfItem it, int lane) {
+    constexpr int NB = 4;
+    int const M = it.m, N = it.n, lda = it.lda;
+    double* a = it.a;
+    int32_t* ipiv = it.ipiv;
+    int k = 0;
+    for (; k + NB < M && k + NB < N; k += NB) {
+        int const r = warp_getf2(a, lda, k, k, M - k, NB, ipiv + k, lane);
+        __syncwarp();
+        if (lane < NB) ipiv[k + lane] += k;
+        __syncwarp();
+        if (r) return k + r;
+        warp_laswp(a, lda, 0, k, k, k + NB, ipiv, lane);
+        warp_laswp(a, lda, k + NB, N, k, k + NB, ipiv, lane);
+        __syncwarp();
+        // U12 := L11^{-1} A12, lane per column (trsm<Lower, unit>, scalar order).
+        for (int j = k + NB + lane; j < N; j += 32) {
+            double* cj = a + (int64_t)j * lda;
+            double x[NB];
+#pragma unroll
+            for (int i = 0; i < NB; ++i) {
+                double acc = cj[k + i];
+#pragma unroll
+                for (int q = 0; q < i; ++q) acc = fma(-a[(k + i) + (int64_t)(k + q) * lda], x[q], acc);
+                x[i] = acc;
+                cj[k + i] = acc;
+            }
+        }
+        __syncwarp();
+        // A22 := A22 - A21 * U12 (gemm with K = 4, alpha = -1, beta = 1), lane per element.
+        int const mr = M - k - NB, nr = N - k - NB;
+        int const total = mr * nr;
+        for (int e = lane; e < total; e += 32) {
+            int const i = k + NB + e % mr, j = k + NB + e / mr;
+            double acc = 0.0;
+#pragma unroll
+            for (int q = 0; q < NB; ++q) acc = fma(a[i + (int64_t)(k + q) * lda], a[(k + q) + (int64_t)j * lda], acc);
+            double* c = a + i + (int64_t)j * lda;
+            *c = fma(1.0, *c, -acc);
+        }
+        __syncwarp();
+    }
+    if (k < M && k < N) {
+        int const r = warp_getf2(a, lda, k, k, M - k, N - k, ipiv + k, lane);
+        __syncwarp();
+        for (int i = k + lane; i < M && i < N; i += 32) ipiv[i] += k;
+        __syncwarp();
+        if (r) return k + r;
+    }
+    warp_laswp(a, lda, 0, k, k, min(M, N), ipiv, lane);
+    __syncwarp();
+    return 0;
+}
+
+template <class Batch>
+__global__ void __launch_bounds__(kWarps * 32) getrf_warp_kernel(Batch batch, int64_t count, int32_t* info) {
+    int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int64_t const b = (int64_t)blockIdx.x * kWarps + warp;
+    if (b >= count) return;
+    GetrfItem const it = batch.get(b);
+    int const r = warp_getrf(it, lane);
+    if (info && lane == 0) info[b] = r;
+}
+
+// getrs for one matrix and its right-hand sides, in BLAST's scalar order (dense/Trsm.hpp:39-65):
+// laswp(b) with ipiv[0..n), x_i = b_i - sum_{k<i} l_ik x_k (unit lower), then
+// x_i = (x_i - sum_{k>i, ascending} u_ik x_k) / u_ii.
+__device__ void getrs_thread(int n, int nrhs, const double* a, int lda, const int32_t* ipiv,
+                             double* x, int ldx) {
+    for (int j = 0; j < nrhs; ++j) {
+        double* xj = x + (int64_t)j * ldx;
+        for (int k = 0; k < n; ++k) {
+            int const q = ipiv[k];
+            if (q != k) {
+                double const t = xj[k];
+                xj[k] = xj[q];
+                xj[q] = t;
+            }
+        }
+        for (int i = 0; i < n; ++i) {
+            double acc = xj[i];
+            for (int k = 0; k < i; ++k) acc = fma(-a[i + (int64_t)k * lda], xj[k], acc);
+            xj[i] = acc;
+        }
+        for (int i = n; i-- > 0;) {
+            double acc = xj[i];
+            for (int k = i + 1; k < n; ++k) acc = fma(-a[i + (int64_t)k * lda], xj[k], acc);
+            xj[i] = acc / a[i + (int64_t)i * lda];
+        }
+    }
+}
+
+struct GetrsItem {
+    const double* a;
+    int n, lda;
+    const int32_t* ipiv;
+    double* x;
+    int nrhs, ldx;
+};
+
+struct StridedGetrs {
+    int n, nrhs, lda, ldx;
+    const double* A;
+    int64_t sa;
+    const int32_t* ipiv;
+    int64_t sp;
+    double* X;
+    int64_t sx;
+    __device__ GetrsItem get(int64_t b) const {
+        return {A + b * sa, n, lda, ipiv + b * sp, X + b * sx, nrhs, ldx};
+    }
+};
+
+struct DescGetrs {
+    const blastgpu_getrf_desc* desc;
+    __device__ GetrsItem get(int64_t b) const {
+        blastgpu_getrf_desc const& d = desc[b];
+        return {d.A.data, d.A.rows, d.A.ld, d.ipiv, d.B.data, d.B.cols, d.B.ld};
+    }
+};
+
+template <class Batch>
+__global__ void __launch_bounds__(128) getrs_thread_kernel(Batch batch, int64_t count, const int32_t* info) {
+    int64_t const b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= count) return;
+    if (info && info[b] != 0) return;  // singular factor: BLAST would have thrown in getrf
+    GetrsItem const it = batch.get(b);
+    getrs_thread(it.n, it.nrhs, it.a, it.lda, it.ipiv, it.x, it.ldx);
+}
+
+template <class Batch>
+int launch_getrf(Batch const& batch, int64_t count, int32_t* info, cudaStream_t s) {
+    int64_t const blocks = (count + kWarps - 1) / kWarps;
+    if (blocks > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
+    getrf_warp_kernel<<<(unsigned)blocks, kWarps * 32, 0, s>>>(batch, count, info);
+    return check_launch();
+}
+
+template <class Batch>
+int launch_getrs(Batch const& batch, int64_t count, const int32_t* info, cudaStream_t s) {
+    int64_t const blocks = (count + 127) / 128;
+    if (blocks > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
+    getrs_thread_kernel<<<(unsigned)blocks, 128, 0, s>>>(batch, count, info);
+    return check_launch();
+}
+
+}  // namespace
+}  // namespace blastgpu
+
+using namespace blastgpu;
+
+extern "C" {
+
+int blastgpu_dgetrf_strided(int m, int n, double* A, int lda, int64_t stride_a, int32_t* ipiv,
+                            int64_t stride_ipiv, int32_t* info, int64_t batch, blastgpu_stream_t stream) {
+    if (m < 0) return -1;
+    if (n < 0) return -2;
+    if (m > 0 && n > 0 && !A) return -3;
+    if (lda < (m > 0 ? m : 1)) return -4;
+    if (m > 0 && n > 0 && !ipiv) return -6;
+    if (batch < 0) return -9;
+    if (batch == 0) return BLASTGPU_SUCCESS;
+    if (m == 0 || n == 0) {
+        if (info) {
+            cudaError_t const e = cudaMemsetAsync(info, 0, sizeof(int32_t) * batch, as_cuda(stream));
+            if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
+        }
+        return BLASTGPU_SUCCESS;
+    }
+    StridedGetrf g{m, n, lda, A, stride_a, ipiv, stride_ipiv};
+    return launch_getrf(g, batch, info, as_cuda(stream));
+}
+
+int blastgpu_dgetrf_batched(const blastgpu_getrf_desc* desc, int32_t* info, int64_t batch,
+                            blastgpu_stream_t stream) {
+    if (batch < 0) return -3;
+    if (batch == 0) return BLASTGPU_SUCCESS;
+    if (!desc) return -1;
+    return launch_getrf(DescGetrf{desc}, batch, info, as_cuda(stream));
+}
+
+int blastgpu_dgetrs_strided(int n, int nrhs, const double* LU, int lda, int64_t stride_a,
+                            const int32_t* ipiv, int64_t stride_ipiv, double* X, int ldx,
+                            int64_t stride_x, const int32_t* info, int64_t batch,
+                            blastgpu_stream_t stream) {
+    if (n < 0) return -1;
+    if (nrhs < 0) return -2;
+    if (n > 0 && !LU) return -3;
+    if (lda < (n > 0 ? n : 1)) return -4;
+    if (n > 0 && !ipiv) return -6;
+    if (n > 0 && nrhs > 0 && !X) return -8;
+    if (ldx < (n > 0 ? n : 1)) return -9;
+    if (batch < 0) return -12;
+    if (batch == 0 || n == 0 || nrhs == 0) return BLASTGPU_SUCCESS;
+    StridedGetrs g{n, nrhs, lda, ldx, LU, stride_a, ipiv, stride_ipiv, X, stride_x};
+    return launch_getrs(g, batch, info, as_cuda(stream));
+}
+
+int blastgpu_dgetrs_batched(const blastgpu_getrf_desc* desc, const int32_t* info, int64_t batch,
+                            blastgpu_stream_t stream) {
+    if (batch < 0) return -3;
+    if (batch == 0) return BLASTGPU_SUCCESS;
+    if (!desc) return -1;
+    return launch_getrs(DescGetrs{desc}, batch, info, as_cuda(stream));
+}
+
+int blastgpu_dgesv_batched(const blastgpu_getrf_desc* desc, int32_t* info, int64_t batch,
+                           blastgpu_stream_t stream) {
+    int st = blastgpu_dgetrf_batched(desc, info, batch, stream);
+    if (st != BLASTGPU_SUCCESS) return st;
+    return blastgpu_dgetrs_batched(desc, info, batch, stream);
+}
+
+}  // extern "C"

@@ -17,6 +17,12 @@ GEMM_DTYPE = np.dtype([("A", MAT_DTYPE), ("B", MAT_DTYPE), ("C", MAT_DTYPE), ("D
 assert GEMM_DTYPE.itemsize == 144
 
 
+GETRF_DTYPE = np.dtype([("A", MAT_DTYPE), ("ipiv", "<u8"), ("B", MAT_DTYPE)], align=True)
+assert GETRF_DTYPE.itemsize == 72
+
+EMPTY_MAT = (0, 0, 0, 1, 0, 0, 0)
+
+
 def mat_record(t: torch.Tensor) -> tuple:
     """(data, rows, cols, ld, layout, ps, reserved) for a 2-D float64 CUDA tensor view."""
     from .blast import _as_mat

@@ -78,6 +78,12 @@ int blastgpu_last_cuda_error(void);        /* cudaError_t of the last BLASTGPU_E
 /* Number of kernels this library has launched since load (all threads); for launch accounting. */
 int64_t blastgpu_launch_count(void);
 
+/* Kernel-selection parameters (no BLAST counterpart): the autotuner stores its per-size-bin
+ * choices here (process-wide). Keys are documented beside the entry points they affect; an
+ * unknown key is stored and ignored. tune_get returns -1 for a key that was never set. */
+int blastgpu_tune_set(const char* key, int value);
+int blastgpu_tune_get(const char* key, int* value);
+
 /* Diagnostics (no BLAST counterpart). selftest_recip: y[i] = 1/sqrt(x[i]) (which = 0) or 1/x[i]
  * (which = 1) with the library's Newton-Raphson helpers, device arrays. probe_fp64_tflops:
  * measures the device's binary64 FMA throughput (TFLOP/s) on `stream` and synchronises it. */
@@ -135,6 +141,41 @@ int blastgpu_dpotrs_strided(int n, int nrhs, const double* L, int ldl, int64_t s
                             const double* B, int ldb, int64_t stride_b,
                             double* X, int ldx, int64_t stride_x,
                             int64_t batch, blastgpu_stream_t stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * getrf: LU factorisation with partial pivoting, A = P*L*U, of column-major m x n matrices.
+ * Replaces blast::getrf(A, ipiv) (dense/Getrf.hpp:52-119; its row-major overload does not pivot
+ * and has no counterpart here). ipiv receives min(m, n) 0-based absolute pivot rows (BLAST's
+ * size_t ipiv[], here int32). info[b] = 0, or k+1 for the first exactly-zero pivot (BLAST throws
+ * std::invalid_argument "Matrix is singular", dense/Getf2.hpp:68-69); A and ipiv of such an
+ * instance are unspecified, as after BLAST's exception. Factors and pivots are bit-identical to
+ * BLAST's algorithm (same operations in the same order, IEEE division by the pivot).
+ * ------------------------------------------------------------------------------------------- */
+int blastgpu_dgetrf_strided(int m, int n, double* A, int lda, int64_t stride_a, int32_t* ipiv,
+                            int64_t stride_ipiv, int32_t* info, int64_t batch, blastgpu_stream_t stream);
+
+/* getrs: X := A^{-1} X from getrf's factors: laswp(X, ipiv), trsm<Lower, unit>, trsm<Upper>
+ * (BLAST has no getrs; dense/Laswp.hpp:37-43 and dense/Trsm.hpp:17-66 in BLAST's order).
+ * Instances whose info entry is non-zero are skipped (info may be NULL). */
+int blastgpu_dgetrs_strided(int n, int nrhs, const double* LU, int lda, int64_t stride_a,
+                            const int32_t* ipiv, int64_t stride_ipiv, double* X, int ldx,
+                            int64_t stride_x, const int32_t* info, int64_t batch,
+                            blastgpu_stream_t stream);
+
+/* Ragged batches: one descriptor per instance, device-resident. A must be column-major. */
+typedef struct blastgpu_getrf_desc {
+    blastgpu_mat A;  /* m x n, overwritten by L and U */
+    int32_t* ipiv;   /* min(m, n) pivots */
+    blastgpu_mat B;  /* n x nrhs right-hand sides, overwritten by X (getrs / gesv only) */
+} blastgpu_getrf_desc; /* 72 bytes */
+
+int blastgpu_dgetrf_batched(const blastgpu_getrf_desc* desc, int32_t* info, int64_t batch,
+                            blastgpu_stream_t stream);
+int blastgpu_dgetrs_batched(const blastgpu_getrf_desc* desc, const int32_t* info, int64_t batch,
+                            blastgpu_stream_t stream);
+/* getrf followed by getrs on every instance (two launches on `stream`). */
+int blastgpu_dgesv_batched(const blastgpu_getrf_desc* desc, int32_t* info, int64_t batch,
+                           blastgpu_stream_t stream);
 
 #ifdef __cplusplus
 }

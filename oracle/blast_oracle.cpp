@@ -182,9 +182,105 @@ int potrf_impl(int M, int N, MA A, ML L, int kn, int tile) {
     return info;
 }
 
-// Fast column-major variant for the batch driver (same arithmetic as potrf_impl with kn = tile = 4).
-int potrf_col(int n, double* A, int64_t lda, double* L, int64_t ldl) {
-    return potrf_impl(n, n, Col{A, lda}, Col{L, ldl}, 4, 4);
+// Column-major Cholesky for the batch driver, shaped like BLAST's kernel (dense/Potrf.hpp:20-106):
+// per strip of 4 columns, register tiles of KM = 12/8/4 rows whose inner loops run over
+// contiguous rows, so the compiler vectorises them the way BLAST's SIMD tiles are. Same
+// per-element operations, in the same order, as potrf_impl (tile = kn = 4): bitwise identical.
+template <int KM>
+void potrf_tile_col(int n, int k, int i, int nc, const double* A, int64_t lda, double* L, int64_t ldl,
+                    double* sq, bool diag, int& info) {
+    double acc[4][KM];
+    int const nr = std::min(KM, n - i);
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < KM; ++r)
+            acc[c][r] = (c < nc && r < nr) ? A[(i + r) + (k + c) * lda] : 0.0;
+    if (nr == KM && nc == 4) {
+        for (int l = 0; l < k; ++l) {
+            const double* a = L + i + l * ldl;
+            double const b0 = L[k + l * ldl], b1 = L[k + 1 + l * ldl];
+            double const b2 = L[k + 2 + l * ldl], b3 = L[k + 3 + l * ldl];
+            for (int r = 0; r < KM; ++r) {
+                double const ar = -a[r];
+                acc[0][r] = std::fma(ar, b0, acc[0][r]);
+                acc[1][r] = std::fma(ar, b1, acc[1][r]);
+                acc[2][r] = std::fma(ar, b2, acc[2][r]);
+                acc[3][r] = std::fma(ar, b3, acc[3][r]);
+            }
+        }
+    } else {
+        for (int l = 0; l < k; ++l)
+            for (int c = 0; c < nc; ++c) {
+                double const b = L[k + c + l * ldl];
+                for (int r = 0; r < nr; ++r) acc[c][r] = std::fma(-L[i + r + l * ldl], b, acc[c][r]);
+            }
+    }
+    for (int c = 0; c < nc; ++c) {
+        for (int j = 0; j < c; ++j) {
+            double const lcj = diag ? acc[j][c] : L[(k + c) + (k + j) * ldl];
+            for (int r = 0; r < KM; ++r) acc[c][r] = std::fma(-lcj, acc[j][r], acc[c][r]);
+        }
+        if (diag) {
+            double const s = acc[c][c];
+            if (!(s > 0.0) && info == 0) info = k + c + 1;
+            sq[c] = std::sqrt(s);
+            for (int r = 0; r < KM; ++r) acc[c][r] = acc[c][r] / sq[c];
+        } else {
+            double const d = L[(k + c) + (k + c) * ldl];
+            for (int r = 0; r < KM; ++r) acc[c][r] = acc[c][r] / d;
+        }
+    }
+    for (int c = 0; c < nc; ++c)
+        for (int r = diag ? c : 0; r < nr; ++r) L[(i + r) + (k + c) * ldl] = acc[c][r];
+}
+
+int potrf_col(int n, const double* A, int64_t lda, double* L, int64_t ldl) {
+    int info = 0;
+    double sq[4];
+    for (int k = 0; k < n; k += 4) {
+        int const nc = std::min(4, n - k);
+        int i = k;
+        while (i < n) {
+            int const rem = n - i;
+            if (rem > 8) { potrf_tile_col<12>(n, k, i, nc, A, lda, L, ldl, sq, i == k, info); i += 12; }
+            else if (rem > 4) { potrf_tile_col<8>(n, k, i, nc, A, lda, L, ldl, sq, i == k, info); i += 8; }
+            else { potrf_tile_col<4>(n, k, i, nc, A, lda, L, ldl, sq, i == k, info); i += 4; }
+        }
+    }
+    return info;
+}
+
+// The two solves of potrs for the batch driver, vectorised across right-hand sides with a
+// row-major scratch copy of X; per element the same order as trsm_impl (dense/Trsm.hpp:39-65).
+constexpr int kMaxRhs = 8;
+void potrs_col(int n, int nrhs, const double* L, int64_t ldl, const double* B, int64_t ldb,
+               double* X, int64_t ldx, double* xr /* n*kMaxRhs scratch */) {
+    for (int j0 = 0; j0 < nrhs; j0 += kMaxRhs) {
+        int const nj = std::min(kMaxRhs, nrhs - j0);
+        for (int i = 0; i < n; ++i) {
+            double acc[kMaxRhs];
+            for (int j = 0; j < nj; ++j) acc[j] = B[i + (j0 + j) * ldb];
+            for (int k = 0; k < i; ++k) {
+                double const a = -L[i + k * ldl];
+                const double* x = xr + k * kMaxRhs;
+                for (int j = 0; j < kMaxRhs; ++j) acc[j] = std::fma(a, x[j], acc[j]);
+            }
+            double const d = L[i + i * ldl];
+            for (int j = 0; j < kMaxRhs; ++j) xr[i * kMaxRhs + j] = j < nj ? acc[j] / d : 0.0;
+        }
+        for (int i = n; i-- > 0;) {
+            double acc[kMaxRhs];
+            for (int j = 0; j < kMaxRhs; ++j) acc[j] = xr[i * kMaxRhs + j];
+            for (int k = i + 1; k < n; ++k) {
+                double const a = -L[k + i * ldl];
+                const double* x = xr + k * kMaxRhs;
+                for (int j = 0; j < kMaxRhs; ++j) acc[j] = std::fma(a, x[j], acc[j]);
+            }
+            double const d = L[i + i * ldl];
+            for (int j = 0; j < kMaxRhs; ++j) xr[i * kMaxRhs + j] = acc[j] / d;
+        }
+        for (int j = 0; j < nj; ++j)
+            for (int i = 0; i < n; ++i) X[i + (j0 + j) * ldx] = xr[i * kMaxRhs + j];
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -501,11 +597,13 @@ int oracle_dposv_batch(int n, int nrhs, int64_t batch, const double* A, int64_t 
 #pragma omp parallel for schedule(dynamic, 16) num_threads(threads)
 #endif
     for (int64_t b = 0; b < batch; ++b) {
+        thread_local std::vector<double> scratch;
+        if ((int)scratch.size() < n * kMaxRhs) scratch.resize((size_t)n * kMaxRhs);
         double* l = L + b * sa;
         double* x = X + b * sb;
-        int const r = potrf_impl(n, n, Col{const_cast<double*>(A) + b * sa, n}, Col{l, n}, 4, 4);
+        int const r = potrf_col(n, A + b * sa, n, l, n);
         if (info) info[b] = r;
-        potrs_impl(n, nrhs, Col{l, n}, Col{const_cast<double*>(B) + b * sb, n}, Col{x, n});
+        if (nrhs > 0) potrs_col(n, nrhs, l, n, B + b * sb, n, x, n, scratch.data());
     }
     return 0;
 }

@@ -70,6 +70,8 @@ def mat(a: np.ndarray) -> oracle_mat:
     if a.dtype != np.float64 or a.ndim != 2:
         raise TypeError("float64 2-D array expected")
     r, c = a.shape
+    if r == 0 or c == 0:
+        return oracle_mat(a.ctypes.data, r, c, max(r, 1), 0, 0, 0)
     s0, s1 = (s // 8 for s in a.strides)
     if s0 == 1 and (s1 >= max(r, 1) or c <= 1):
         return oracle_mat(a.ctypes.data, r, c, max(s1, r, 1), 0, 0, 0)
