@@ -123,6 +123,86 @@ def peak_fp64_tflops() -> float:
     return out.value
 
 
+def make_mixed_inputs(count: int, seed: int, device):
+    """The mixed-precision workload: n ~ U{64..512}; A = Q diag(lambda) Q^T with Q from the QR of a
+    seeded Gaussian and lambda log-spaced so that cond(A) is 1e2, 1e4 or 1e6 (a third each);
+    one N(0,1) right-hand side. Built on the device in binary64, grouped by size."""
+    import numpy as np
+    import torch
+
+    from blast_gb300.ragged import Packed
+
+    rng = np.random.default_rng(seed)
+    ns = rng.integers(64, 513, count)
+    conds = np.array([1e2, 1e4, 1e6])[np.arange(count) % 3]
+    A = Packed(ns, ns, device)
+    B = Packed(ns, np.ones_like(ns), device)
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    for n in np.unique(ns):
+        idx = np.nonzero(ns == n)[0]
+        G = torch.randn(len(idx), n, n, generator=g, device=device, dtype=torch.float64)
+        Q, _ = torch.linalg.qr(G)
+        lam = torch.stack([torch.logspace(0, -float(np.log10(conds[i])), n, device=device,
+                                          dtype=torch.float64) for i in idx])
+        M = (Q * lam[:, None, :]) @ Q.mT
+        M = 0.5 * (M + M.mT)
+        for j, i in enumerate(idx):
+            A.view(int(i)).copy_(M[j])
+        del G, Q, M
+    B.buf.copy_(torch.randn(B.buf.numel(), generator=g, device=device, dtype=torch.float64))
+    return ns, conds, A, B
+
+
+def mixed_ir_comparison(steps: int, count: int = 8192):
+    """FP64 vs mixed-precision + refinement on the ragged n in [64, 512] batch (one CTA per
+    matrix, one launch per step for each path)."""
+    import numpy as np
+    import torch
+
+    from blast_gb300.ragged import Packed, PosvPlan
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    ns, conds, A, B = make_mixed_inputs(count, 4321, dev)
+    ones = np.ones_like(ns)
+    X64, X32 = Packed(ns, ones, dev), Packed(ns, ones, dev)
+    L = Packed(ns, ns, dev)
+    p64 = PosvPlan(A, B, X64, L)
+    pmx = PosvPlan(A, B, X32, mixed=True, tol=1e-12, max_iter=10)
+    flops = float(np.sum(ns.astype(np.float64) ** 3 / 3 + ns ** 2 / 2 + ns / 6 + 2 * ns ** 2))
+    out = {}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for name, plan, k in (("fp64", p64, max(1, steps // 4)), ("mixed", pmx, steps)):
+        plan.run()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(k):
+            plan.run()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / k
+        out[name] = {"ms_per_step": ms, "matrices_per_s": count / ms * 1e3,
+                     "gflops_nominal": flops / ms / 1e6, "steps": k}
+    info, iters, berr = pmx.results()
+    info64, _, _ = p64.results()
+    # backward error of the binary64 path, computed on the device
+    be64 = []
+    for i in range(0, count, max(1, count // 64)):
+        a, b, x = A.view(i), B.view(i), X64.view(i)
+        r = b - a @ x
+        be64.append(float(r.abs().max() / (a.abs().sum(1).max() * x.abs().max() + b.abs().max())))
+    out["mixed"].update({"max_backward_error": float(np.max(berr)),
+                         "converged": int(np.sum((berr <= 1e-12) & (info == 0))),
+                         "iterations_histogram": {int(k): int(v) for k, v in zip(*np.unique(iters, return_counts=True))},
+                         "factorisation_breakdowns": int(np.sum(info != 0))})
+    out["fp64"]["sampled_max_backward_error"] = float(np.max(be64))
+    out["fp64"]["info_nonzero"] = int(np.sum(info64 != 0))
+    out["speedup_matrices_per_s"] = out["mixed"]["matrices_per_s"] / out["fp64"]["matrices_per_s"]
+    out["workload"] = (f"{count} SPD matrices, n ~ U{{64..512}}, A = Q diag(lambda) Q^T, "
+                       "cond in {1e2,1e4,1e6}, 1 RHS; tol 1e-12")
+    return out
+
+
 def load_traffic():
     p = ROOT / "profiles" / "posv_n48_traffic.json"
     if p.exists():
@@ -305,6 +385,8 @@ def run_ours(args):
                             "frac": gbs / hbm if hbm else None}
     if ws == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline()
+    if not args.no_mixed:
+        line["mixed_ir"] = mixed_ir_comparison(max(4, min(args.steps, 20)))
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
@@ -320,6 +402,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true",
                     help="device-timed leg only (small profiling runs); prints a reduced line")
     ap.add_argument("--batch", type=int, default=BATCH, help="matrices per GPU (default 50,000)")
+    ap.add_argument("--no-mixed", action="store_true",
+                    help="skip the FP64-vs-mixed comparison on the ragged n in [64, 512] batch")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -1,0 +1,459 @@
+// Ragged batched Cholesky solve for medium sizes (one CTA per matrix), binary64 and
+// mixed precision (binary32 factorisation + binary64 iterative refinement), sm_103a.
+//
+// Reference: blast::potrf (dense/Potrf.hpp:66-106) is left-looking: each column strip is first
+// updated with all previous columns (the ger(-1, ...) loop, a gemm), then factored on the
+// diagonal and solved below it (RegisterMatrix::potrf / ::trsm). The solves are BLAST's trsm
+// (dense/Trsm.hpp:17-66). BLAST has no mixed precision and no refinement; that part is new.
+//
+// GPU mapping: one CTA of 256 threads (8 warps) per matrix, the whole solve in one launch.
+//  * Factorisation, left-looking with panels of 32 columns. Warp w owns panel columns
+//    4w..4w+3, lane l owns rows l, l+32, ..., so each thread keeps an MAXR x 4 register tile
+//    (BLAST's RegisterMatrix, 32 times wider). The update of a panel with all previous columns
+//    streams those columns through shared memory 16 at a time; every thread then performs
+//    MAXR*4 fused multiply-adds per column with operands read conflict-free from shared memory
+//    (rows: consecutive lanes; panel columns: a warp-uniform broadcast).
+//  * The 32 x 32 diagonal block is factored in place in shared memory (right-looking, all
+//    threads), the rows below are solved against it (one thread per row), and the panel is
+//    written to the factor.
+//  * Forward and backward substitution run blockwise: a warp solves each 32 x 32 triangle with
+//    shuffles, then all threads apply the block to the remaining rows.
+//  * Mixed precision: the factor is binary32 (in the caller's workspace); the residual
+//    r = b - A*x is computed in binary64 from A's lower triangle, the correction solve uses the
+//    binary32 factor on the scaled residual, and each matrix iterates until its normwise
+//    backward error |r|_inf / (|A|_inf |x|_inf + |b|_inf) reaches the tolerance.
+// On GB300 binary32 FMAs issue ~58x faster than binary64 (70 vs 1.2 TFLOP/s measured), which is
+// what the mixed path turns into matrices per second.
+#include <math_constants.h>
+
+#include "common.cuh"
+
+namespace blastgpu {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kNB = 32;  // panel width = 4 columns per warp
+constexpr int kKC = 16;  // previous columns staged per pass of the panel update
+
+struct CtaItem {
+    int n;
+    const double* A; int lda;
+    double* L; int ldl;       // binary64 factor output (plain path) or nullptr
+    const double* B; int ldb;
+    double* X; int ldx;
+    int nrhs;
+    char* ws;                 // per-instance workspace (mixed path)
+};
+
+struct DescPosv {
+    const blastgpu_posv_desc* desc;
+    char* workspace;
+    __device__ CtaItem get(int64_t b) const {
+        blastgpu_posv_desc const& d = desc[b];
+        return {d.A.rows, d.A.data, d.A.ld, d.L.data, d.L.ld, d.B.data, d.B.ld,
+                d.X.data, d.X.ld, d.B.cols, workspace ? workspace + d.ws_offset : nullptr};
+    }
+};
+
+template <typename T>
+__device__ __forceinline__ T rsqrt_t(T s);
+template <>
+__device__ __forceinline__ double rsqrt_t<double>(double s) { return rsqrt_nr(s); }
+template <>
+__device__ __forceinline__ float rsqrt_t<float>(float s) { return 1.0f / sqrtf(s); }
+
+template <typename T>
+__device__ __forceinline__ T rcp_t(T s);
+template <>
+__device__ __forceinline__ double rcp_t<double>(double s) { return rcp_nr(s); }
+template <>
+__device__ __forceinline__ float rcp_t<float>(float s) { return 1.0f / s; }
+
+// Shared-memory layout (T = factor precision):
+//   union { stage[kKC][NMAX] (panel update) ; panel[kNB][NMAX] (diag + trsm) }
+//   vecs: 4 * NMAX doubles (b/x, r, work) + reductions
+template <typename T, int MAXR>
+struct Smem {
+    static constexpr int NMAX = 32 * MAXR;
+    static constexpr int kPanelElems = kNB * NMAX;
+    static constexpr int kStageElems = kKC * NMAX;
+    static constexpr int kBufElems = kPanelElems > kStageElems ? kPanelElems : kStageElems;
+    static constexpr size_t kBytes = sizeof(T) * kBufElems + sizeof(double) * (4 * NMAX + 64);
+};
+
+// Left-looking blocked Cholesky of the n x n matrix: lower(A) -> F (precision T, ld ldf).
+// Returns info (0 or first bad pivot + 1) identically in all threads.
+template <typename T, int MAXR>
+__device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf, int* s_info) {
+    constexpr int NMAX = 32 * MAXR;
+    int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) *s_info = 0;
+    for (int k0 = 0; k0 < n; k0 += kNB) {
+        int const nb = min(kNB, n - k0);
+        int const m = n - k0;
+        int const c0 = warp * 4;  // this warp's panel columns c0..c0+3 (relative to k0)
+        T acc[MAXR][4];
+#pragma unroll
+        for (int i = 0; i < MAXR; ++i) {
+            int const r = lane + 32 * i;  // row relative to k0
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                int const c = c0 + j;
+                acc[i][j] = (r < m && c < nb && r >= c) ? (T)A[(k0 + r) + (int64_t)(k0 + c) * lda] : (T)0;
+            }
+        }
+        // Panel update with the previous columns: acc -= F(k0:n, kk) * F(k0+c, kk)
+        for (int kk = 0; kk < k0; kk += kKC) {
+            int const kc = min(kKC, k0 - kk);
+            __syncthreads();
+            for (int idx = tid; idx < kc * m; idx += kThreads) {
+                int const q = idx / m, r = idx - q * m;
+                buf[q * NMAX + r] = F[(k0 + r) + (int64_t)(kk + q) * ldf];
+            }
+            __syncthreads();
+            for (int q = 0; q < kc; ++q) {
+                T const* col = buf + q * NMAX;
+                T b[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) b[j] = (c0 + j < nb) ? col[c0 + j] : (T)0;
+#pragma unroll
+                for (int i = 0; i < MAXR; ++i) {
+                    int const r = lane + 32 * i;
+                    if (i * 32 < m) {
+                        T const a = r < m ? col[r] : (T)0;
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) acc[i][j] = fma(-a, b[j], acc[i][j]);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        // Panel to shared memory, column-major with stride NMAX.
+#pragma unroll
+        for (int i = 0; i < MAXR; ++i) {
+            int const r = lane + 32 * i;
+            if (r < m) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (c0 + j < nb) buf[(c0 + j) * NMAX + r] = acc[i][j];
+            }
+        }
+        __syncthreads();
+        // Diagonal block: right-looking Cholesky in shared memory.
+        for (int j = 0; j < nb; ++j) {
+            T* cj = buf + j * NMAX;
+            T const d = cj[j];
+            if (!(d > (T)0) && tid == 0 && *s_info == 0) *s_info = k0 + j + 1;
+            T const y = rsqrt_t<T>(d);
+            // column j below the diagonal, inside the block and below it (the panel trsm is
+            // folded into the same right-looking sweep)
+            for (int r = j + 1 + tid; r < m; r += kThreads) cj[r] *= y;
+            __syncthreads();
+            // Every thread has read d by now and nothing below reads cj[j] again.
+            if (tid == 0) cj[j] = d * y;
+            // trailing columns of the panel: buf[l][r] -= buf[j][r] * buf[j][l], r >= l > j
+            int const rest = nb - j - 1;
+            for (int idx = tid; idx < rest * m; idx += kThreads) {
+                int const l = j + 1 + idx / m, r = idx % m;
+                if (r >= l) buf[l * NMAX + r] = fma(-cj[r], cj[l], buf[l * NMAX + r]);
+            }
+            __syncthreads();
+        }
+        // Panel to the factor (lower part).
+        for (int idx = tid; idx < nb * m; idx += kThreads) {
+            int const c = idx / m, r = idx - c * m;
+            if (r >= c) F[(k0 + r) + (int64_t)(k0 + c) * ldf] = buf[c * NMAX + r];
+        }
+        __syncthreads();
+    }
+    return *s_info;
+}
+
+// In-place solve with the factor: v := F^{-T} F^{-1} v (v in shared memory, precision T).
+template <typename T, int MAXR>
+__device__ void cta_potrs(int n, const T* F, int ldf, T* v) {
+    int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // forward: F * y = v
+    for (int j0 = 0; j0 < n; j0 += 32) {
+        int const nb = min(32, n - j0);
+        if (warp == 0) {
+            T x = lane < nb ? v[j0 + lane] : (T)0;
+            for (int j = 0; j < nb; ++j) {
+                T const fjj = F[(j0 + j) + (int64_t)(j0 + j) * ldf];
+                T xj = __shfl_sync(0xffffffffu, x, j);
+                xj = xj * rcp_t<T>(fjj);
+                if (lane == j) x = xj;
+                if (lane > j && lane < nb) x = fma(-F[(j0 + lane) + (int64_t)(j0 + j) * ldf], xj, x);
+            }
+            if (lane < nb) v[j0 + lane] = x;
+        }
+        __syncthreads();
+        for (int r = j0 + nb + tid; r < n; r += kThreads) {
+            T acc = v[r];
+            for (int j = 0; j < nb; ++j) acc = fma(-F[r + (int64_t)(j0 + j) * ldf], v[j0 + j], acc);
+            v[r] = acc;
+        }
+        __syncthreads();
+    }
+    // backward: F^T * x = y, blocks from the bottom
+    int const last = ((n - 1) / 32) * 32;
+    for (int j0 = last; j0 >= 0; j0 -= 32) {
+        int const nb = min(32, n - j0);
+        // rows of this block get the contributions of the rows below it: v_i -= sum_r F(r,i) v_r
+        if (j0 + nb < n) {
+            // each warp takes columns i of the block; lanes split r with a shuffle reduction
+            for (int i = warp; i < nb; i += kWarps) {
+                T acc = (T)0;
+                for (int r = j0 + nb + lane; r < n; r += 32) acc = fma(F[r + (int64_t)(j0 + i) * ldf], v[r], acc);
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+                if (lane == 0) v[j0 + i] -= acc;
+            }
+            __syncthreads();
+        }
+        if (warp == 0) {
+            T x = lane < nb ? v[j0 + lane] : (T)0;
+            for (int j = nb - 1; j >= 0; --j) {
+                T const fjj = F[(j0 + j) + (int64_t)(j0 + j) * ldf];
+                T xj = __shfl_sync(0xffffffffu, x, j);
+                xj = xj * rcp_t<T>(fjj);
+                if (lane == j) x = xj;
+                if (lane < j) x = fma(-F[(j0 + j) + (int64_t)(j0 + lane) * ldf], xj, x);
+            }
+            if (lane < nb) v[j0 + lane] = x;
+        }
+        __syncthreads();
+    }
+}
+
+// Block-wide max reduction of non-negative values (NaN propagates as the result).
+__device__ __forceinline__ double cta_max(double v, double* red) {
+    int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        double const o = __shfl_xor_sync(0xffffffffu, v, off);
+        v = (o > v || o != o) ? o : v;
+    }
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double r = red[0];
+    for (int w = 1; w < kWarps; ++w) r = (red[w] > r || red[w] != red[w]) ? red[w] : r;
+    return r;
+}
+
+// y = A*x for symmetric A given by its lower triangle (binary64); x, y in shared memory.
+__device__ void cta_symv_lower(int n, const double* A, int lda, const double* x, double* y) {
+    int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // y_i = sum_{j<=i} A(i,j) x_j   (thread per row, coalesced down each column)
+    for (int i = tid; i < n; i += kThreads) {
+        double acc = 0.0;
+        for (int j = 0; j <= i; ++j) acc = fma(A[i + (int64_t)j * lda], x[j], acc);
+        y[i] = acc;
+    }
+    __syncthreads();
+    // y_i += sum_{j>i} A(j,i) x_j   (warp per column, lanes down the column)
+    for (int i = warp; i < n; i += kWarps) {
+        double acc = 0.0;
+        for (int j = i + 1 + lane; j < n; j += 32) acc = fma(A[j + (int64_t)i * lda], x[j], acc);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+        if (lane == 0) y[i] += acc;
+    }
+    __syncthreads();
+}
+
+struct CtaArgs {
+    int64_t batch;
+    int32_t* info;
+    int32_t* iters;
+    double* berr;
+    double tol;
+    int max_iter;
+};
+
+// Plain binary64 path: factor into L, then X = A^{-1} B column by column.
+template <int MAXR, class Batch>
+__global__ void __launch_bounds__(kThreads, 1) posv_cta_f64_kernel(Batch batch, CtaArgs args) {
+    using S = Smem<double, MAXR>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double* buf = reinterpret_cast<double*>(smem_raw);
+    double* vec = buf + S::kBufElems;
+    __shared__ int s_info;
+    int64_t const b = blockIdx.x;
+    if (b >= args.batch) return;
+    CtaItem const it = batch.get(b);
+    int const n = it.n;
+    int const info = cta_potrf<double, MAXR>(n, it.A, it.lda, it.L, it.ldl, buf, &s_info);
+    if (threadIdx.x == 0 && args.info) args.info[b] = info;
+    for (int c = 0; c < it.nrhs; ++c) {
+        for (int i = threadIdx.x; i < n; i += kThreads) vec[i] = it.B[i + (int64_t)c * it.ldb];
+        __syncthreads();
+        cta_potrs<double, MAXR>(n, it.L, it.ldl, vec);
+        for (int i = threadIdx.x; i < n; i += kThreads) it.X[i + (int64_t)c * it.ldx] = vec[i];
+        __syncthreads();
+    }
+}
+
+// Mixed path: binary32 factor in the workspace, binary64 refinement.
+template <int MAXR, class Batch>
+__global__ void __launch_bounds__(kThreads, 2) posv_cta_mixed_kernel(Batch batch, CtaArgs args) {
+    using S = Smem<float, MAXR>;
+    constexpr int NMAX = S::NMAX;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* buf = reinterpret_cast<float*>(smem_raw);
+    double* x = reinterpret_cast<double*>(smem_raw + sizeof(float) * S::kBufElems);
+    double* r = x + NMAX;
+    double* bb = r + NMAX;
+    float* w = reinterpret_cast<float*>(bb + NMAX);  // NMAX floats (fits in the 4th vector)
+    double* red = bb + 2 * NMAX;
+    __shared__ int s_info;
+    int64_t const b = blockIdx.x;
+    if (b >= args.batch) return;
+    CtaItem const it = batch.get(b);
+    int const n = it.n, tid = threadIdx.x;
+    float* F = reinterpret_cast<float*>(it.ws);
+    int const info = cta_potrf<float, MAXR>(n, it.A, it.lda, F, n, buf, &s_info);
+    if (tid == 0 && args.info) args.info[b] = info;
+
+    // |A|_inf from the lower triangle: row sums of |A(i,j)| over j<=i plus column sums below.
+    double anorm;
+    {
+        for (int i = tid; i < n; i += kThreads) {
+            double s = 0.0;
+            for (int j = 0; j <= i; ++j) s += fabs(it.A[i + (int64_t)j * it.lda]);
+            r[i] = s;
+        }
+        __syncthreads();
+        int const lane = tid & 31, warp = tid >> 5;
+        for (int i = warp; i < n; i += kWarps) {
+            double s = 0.0;
+            for (int j = i + 1 + lane; j < n; j += 32) s += fabs(it.A[j + (int64_t)i * it.lda]);
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+            if (lane == 0) r[i] += s;
+        }
+        __syncthreads();
+        double m = 0.0;
+        for (int i = tid; i < n; i += kThreads) m = fmax(m, r[i]);
+        anorm = cta_max(m, red);
+    }
+
+    int total_iters = 0;
+    double worst = 0.0;
+    for (int c = 0; c < it.nrhs; ++c) {
+        double bm = 0.0;
+        for (int i = tid; i < n; i += kThreads) {
+            bb[i] = it.B[i + (int64_t)c * it.ldb];
+            bm = fmax(bm, fabs(bb[i]));
+        }
+        double const bnorm = cta_max(bm, red);
+        // x0 = F^{-T} F^{-1} b in binary32
+        for (int i = tid; i < n; i += kThreads) w[i] = (float)bb[i];
+        __syncthreads();
+        if (info == 0) cta_potrs<float, MAXR>(n, F, n, w);
+        for (int i = tid; i < n; i += kThreads) x[i] = info == 0 ? (double)w[i] : CUDART_NAN;
+        __syncthreads();
+        double be = CUDART_INF;
+        int it_count = 0;
+        for (;;) {
+            // r = b - A x (binary64)
+            cta_symv_lower(n, it.A, it.lda, x, r);
+            double rm = 0.0, xm = 0.0;
+            for (int i = tid; i < n; i += kThreads) {
+                r[i] = bb[i] - r[i];
+                rm = fmax(rm, fabs(r[i]));
+                xm = fmax(xm, fabs(x[i]));
+            }
+            rm = cta_max(rm, red);
+            xm = cta_max(xm, red);
+            double const den = anorm * xm + bnorm;
+            be = den > 0.0 ? rm / den : (rm == 0.0 ? 0.0 : CUDART_INF);
+            if (!(be > args.tol) || it_count >= args.max_iter || info != 0) break;
+            // d = F^{-T} F^{-1} (r / s) * s in binary32, with s = |r|_inf keeping r in range
+            double const s = rm;
+            for (int i = tid; i < n; i += kThreads) w[i] = (float)(r[i] / s);
+            __syncthreads();
+            cta_potrs<float, MAXR>(n, F, n, w);
+            for (int i = tid; i < n; i += kThreads) x[i] += (double)w[i] * s;
+            __syncthreads();
+            ++it_count;
+        }
+        for (int i = tid; i < n; i += kThreads) it.X[i + (int64_t)c * it.ldx] = x[i];
+        __syncthreads();
+        total_iters = max(total_iters, it_count);
+        worst = (be > worst || be != be) ? be : worst;
+    }
+    if (tid == 0) {
+        if (args.iters) args.iters[b] = total_iters;
+        if (args.berr) args.berr[b] = worst;
+    }
+}
+
+template <int MAXR, class Batch>
+int launch_cta(bool mixed, Batch const& batch, CtaArgs const& args, cudaStream_t s) {
+    size_t const smem = mixed ? Smem<float, MAXR>::kBytes : Smem<double, MAXR>::kBytes;
+    cudaError_t e;
+    if (mixed) {
+        e = cudaFuncSetAttribute(posv_cta_mixed_kernel<MAXR, Batch>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) posv_cta_mixed_kernel<MAXR, Batch><<<(unsigned)args.batch, kThreads, smem, s>>>(batch, args);
+    } else {
+        e = cudaFuncSetAttribute(posv_cta_f64_kernel<MAXR, Batch>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) posv_cta_f64_kernel<MAXR, Batch><<<(unsigned)args.batch, kThreads, smem, s>>>(batch, args);
+    }
+    if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
+    return check_launch();
+}
+
+template <class Batch>
+int dispatch_cta(bool mixed, int max_n, Batch const& batch, CtaArgs const& args, cudaStream_t s) {
+    if (args.batch == 0) return BLASTGPU_SUCCESS;
+    if (args.batch > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
+    if (max_n <= 64) return launch_cta<2>(mixed, batch, args, s);
+    if (max_n <= 128) return launch_cta<4>(mixed, batch, args, s);
+    if (max_n <= 256) return launch_cta<8>(mixed, batch, args, s);
+    if (max_n <= 512) return launch_cta<16>(mixed, batch, args, s);
+    return BLASTGPU_ERR_TOO_LARGE;
+}
+
+}  // namespace
+}  // namespace blastgpu
+
+using namespace blastgpu;
+
+extern "C" {
+
+size_t blastgpu_dposv_mixed_workspace_bytes(int n) {
+    if (n <= 0) return 0;
+    size_t const bytes = sizeof(float) * (size_t)n * (size_t)n;
+    return (bytes + 255) & ~(size_t)255;
+}
+
+int blastgpu_dposv_batched(const blastgpu_posv_desc* desc, int64_t batch, int max_n, int32_t* info,
+                           blastgpu_stream_t stream) {
+    if (batch < 0) return -2;
+    if (batch == 0) return BLASTGPU_SUCCESS;
+    if (!desc) return -1;
+    if (max_n < 0) return -3;
+    if (max_n > 512) return BLASTGPU_ERR_TOO_LARGE;
+    CtaArgs a{batch, info, nullptr, nullptr, 0.0, 0};
+    return dispatch_cta(false, max_n, DescPosv{desc, nullptr}, a, as_cuda(stream));
+}
+
+int blastgpu_dposv_mixed_batched(const blastgpu_posv_desc* desc, int64_t batch, int max_n,
+                                 void* workspace, double tol, int max_iter, int32_t* info,
+                                 int32_t* iters, double* berr, blastgpu_stream_t stream) {
+    if (batch < 0) return -2;
+    if (batch == 0) return BLASTGPU_SUCCESS;
+    if (!desc) return -1;
+    if (max_n < 0) return -3;
+    if (max_n > 512) return BLASTGPU_ERR_TOO_LARGE;
+    if (!workspace) return -4;
+    if (!(tol >= 0.0)) return -5;
+    if (max_iter < 0) return -6;
+    CtaArgs a{batch, info, iters, berr, tol, max_iter};
+    return dispatch_cta(true, max_n, DescPosv{desc, static_cast<char*>(workspace)}, a, as_cuda(stream));
+}
+
+}  // extern "C"

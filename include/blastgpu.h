@@ -177,6 +177,35 @@ int blastgpu_dgetrs_batched(const blastgpu_getrf_desc* desc, const int32_t* info
 int blastgpu_dgesv_batched(const blastgpu_getrf_desc* desc, int32_t* info, int64_t batch,
                            blastgpu_stream_t stream);
 
+/* ---------------------------------------------------------------------------------------------
+ * Ragged Cholesky solves, n <= 512, one CTA per matrix, one launch for the whole batch.
+ * Per instance: potrf(A, L) (lower triangle of A read), then X = A^{-1} B (X may alias B).
+ * ------------------------------------------------------------------------------------------- */
+typedef struct blastgpu_posv_desc {
+    blastgpu_mat A;     /* n x n SPD, column-major; lower triangle read */
+    blastgpu_mat L;     /* n x n column-major factor output (binary64 path); unused by the mixed path */
+    blastgpu_mat B;     /* n x nrhs column-major right-hand sides */
+    blastgpu_mat X;     /* n x nrhs column-major solutions */
+    int64_t ws_offset;  /* mixed path: byte offset of this instance's scratch in `workspace`
+                           (blastgpu_dposv_mixed_workspace_bytes(n) bytes, 256-byte aligned) */
+} blastgpu_posv_desc;   /* 136 bytes */
+
+/* Binary64 path (BLAST's arithmetic, divisions as reciprocal multiplications). max_n bounds every
+ * instance's n and selects the register tiling (n <= 64, 128, 256, 512). */
+int blastgpu_dposv_batched(const blastgpu_posv_desc* desc, int64_t batch, int max_n, int32_t* info,
+                           blastgpu_stream_t stream);
+
+/* Mixed precision (no BLAST counterpart): binary32 Cholesky factor, binary64 residuals, binary32
+ * correction solves, iterated per instance until the normwise backward error
+ * |b - A x|_inf / (|A|_inf |x|_inf + |b|_inf) <= tol or max_iter corrections were applied.
+ * Outputs per instance: info (binary32 factorisation breakdown, j+1), iters (corrections
+ * applied, max over right-hand sides), berr (final backward error, max over right-hand sides).
+ * Instances with info != 0 or berr > tol need the binary64 path (the caller re-solves them). */
+size_t blastgpu_dposv_mixed_workspace_bytes(int n);
+int blastgpu_dposv_mixed_batched(const blastgpu_posv_desc* desc, int64_t batch, int max_n,
+                                 void* workspace, double tol, int max_iter, int32_t* info,
+                                 int32_t* iters, double* berr, blastgpu_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -9,7 +9,7 @@ import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
 HEADERS = sorted((ROOT / "include").glob("*.h"))
-DECL = re.compile(r"^\s*(?:const\s+)?(?:int|int64_t|char|void)\s*\*?\s*(blastgpu_\w+)\s*\(", re.M)
+DECL = re.compile(r"^\s*(?:const\s+)?(?:int|int64_t|size_t|char|void)\s*\*?\s*(blastgpu_\w+)\s*\(", re.M)
 
 
 def declared():

@@ -1,0 +1,102 @@
+"""Ragged Cholesky solves (one CTA per matrix): the binary64 path against the oracle and the
+mixed-precision path (binary32 factor + binary64 refinement) against the 1e-12 backward-error bar.
+"""
+import numpy as np
+import pytest
+
+from helpers import EPS, normwise
+
+pytestmark = pytest.mark.gpu
+
+
+def _spd_cond(rng, n, cond):
+    """A = Q diag(lambda) Q^T with lambda log-spaced from 1 to 1/cond (the mixed workload's matrices)."""
+    Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    lam = np.logspace(0, -np.log10(cond), n)
+    A = (Q * lam) @ Q.T
+    return (A + A.T) / 2
+
+
+def test_ragged_posv_fp64_matches_oracle(gpu, oracle_lib):
+    import torch
+
+    from blast_gb300.ragged import Packed, PosvPlan
+
+    rng = np.random.default_rng(0)
+    ns = [65, 1, 7, 32, 33, 64, 100, 128, 129, 200, 256, 257, 300, 511, 512, 31]
+    nrhs = [1, 2, 1, 3, 1, 1, 2, 1, 1, 1, 1, 1, 2, 1, 1, 4]
+    As = [np.tril(rng.standard_normal((n, n))) for n in ns]
+    As = [G @ G.T + n * np.eye(n) for G, n in zip(As, ns)]
+    Bs = [rng.standard_normal((n, r)) for n, r in zip(ns, nrhs)]
+    dev = "cuda"
+    A = Packed(ns, ns, dev)
+    A.fill_from(As)
+    B = Packed(ns, nrhs, dev)
+    B.fill_from(Bs)
+    X = Packed(ns, nrhs, dev)
+    L = Packed(ns, ns, dev)
+    plan = PosvPlan(A, B, X, L)
+    plan.run()
+    torch.cuda.synchronize()
+    info, _, _ = plan.results()
+    assert not info.any()
+    Ls, Xs = L.to_list(), X.to_list()
+    for n, Ah, Bh, Lg, Xg in zip(ns, As, Bs, Ls, Xs):
+        Lr = np.zeros((n, n), order="F")
+        assert oracle_lib.potrf(np.asfortranarray(Ah), Lr) == 0
+        Xr = np.zeros_like(Bh, order="F")
+        oracle_lib.potrs(Lr, np.asfortranarray(Bh), Xr)
+        assert normwise(np.tril(Lg), Lr) <= 10 * n * EPS, n
+        assert normwise(Xg, Xr) <= 100 * n * EPS, n
+
+
+@pytest.mark.parametrize("cond", [1e2, 1e4, 1e6])
+def test_ragged_posv_mixed_backward_error(gpu, cond):
+    import torch
+
+    from blast_gb300.ragged import Packed, PosvPlan
+
+    rng = np.random.default_rng(int(np.log10(cond)))
+    ns = [64, 96, 128, 200, 255, 256, 300, 384, 450, 512]
+    As = [_spd_cond(rng, n, cond) for n in ns]
+    Bs = [rng.standard_normal((n, 1)) for n in ns]
+    A = Packed(ns, ns, "cuda")
+    A.fill_from(As)
+    B = Packed(ns, [1] * len(ns), "cuda")
+    B.fill_from(Bs)
+    X = Packed(ns, [1] * len(ns), "cuda")
+    plan = PosvPlan(A, B, X, mixed=True, tol=1e-12, max_iter=10)
+    plan.run()
+    torch.cuda.synchronize()
+    info, iters, berr = plan.results()
+    assert not info.any()
+    assert np.all(berr <= 1e-12), berr
+    for n, Ah, Bh, Xg in zip(ns, As, Bs, X.to_list()):
+        r = Bh - Ah @ Xg
+        be = np.abs(r).max() / (np.abs(Ah).sum(1).max() * np.abs(Xg).max() + np.abs(Bh).max())
+        assert be <= 1e-12, (n, be)
+        xr = np.linalg.solve(Ah, Bh)
+        assert normwise(Xg, xr) <= 1e-12 * cond * n
+
+
+def test_ragged_posv_mixed_reports_breakdown(gpu):
+    """A matrix that is not positive definite: the mixed path reports info and a huge backward
+    error instead of a solution (the caller re-solves it on the binary64 path)."""
+    import torch
+
+    from blast_gb300.ragged import Packed, PosvPlan
+
+    n = 70
+    A = Packed([n, n], [n, n], "cuda")
+    M = np.eye(n)
+    M[40, 40] = -1.0
+    A.fill_from([np.eye(n) * 2, M])
+    B = Packed([n, n], [1, 1], "cuda")
+    B.fill_from([np.ones((n, 1)), np.ones((n, 1))])
+    X = Packed([n, n], [1, 1], "cuda")
+    plan = PosvPlan(A, B, X, mixed=True)
+    plan.run()
+    torch.cuda.synchronize()
+    info, iters, berr = plan.results()
+    assert info[0] == 0 and berr[0] <= 1e-12
+    assert info[1] == 41 and not (berr[1] <= 1e-12)
