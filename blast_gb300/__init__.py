@@ -5,6 +5,8 @@ build script, a ctypes binding, and ``blast``, a Python mirror of BLAST's functi
 torch device tensors.
 """
 from . import _lib
-from .blast import col_major, gemm, getrf, getrs, posv, potrf, potrs
+from .blast import (LEFT, LOWER, RIGHT, UPPER, col_major, gemm, getrf, getrs, posv, potrf, potrs,
+                    syrk_lower, trmm, trsm)
 
-__all__ = ["gemm", "potrf", "posv", "potrs", "getrf", "getrs", "col_major", "_lib"]
+__all__ = ["gemm", "potrf", "posv", "potrs", "getrf", "getrs", "syrk_lower", "trsm", "trmm",
+           "col_major", "LOWER", "UPPER", "LEFT", "RIGHT", "_lib"]

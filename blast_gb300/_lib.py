@@ -61,8 +61,12 @@ SIGNATURES: dict[str, list] = {
     "blastgpu_dgetrs_batched": [PTR, PTR, I64, PTR],
     "blastgpu_dgesv_batched": [PTR, PTR, I64, PTR],
     "blastgpu_dposv_mixed_workspace_bytes": [I32],
+    "blastgpu_dsyrk_lower_strided": [I32, I32, DBL, PTR, I32, I64, DBL, PTR, I32, I64, PTR, I32, I64, I64, PTR],
+    "blastgpu_dtrsm_strided": [I32, I32, I32, I32, I32, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, I64, PTR],
+    "blastgpu_dtrmm_strided": [I32, I32, I32, I32, I32, DBL, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, I64, PTR],
     "blastgpu_dposv_batched": [PTR, I64, I32, PTR, PTR],
     "blastgpu_dposv_mixed_batched": [PTR, I64, I32, PTR, DBL, I32, PTR, PTR, PTR, PTR],
+    "blastgpu_dposv_bwd_batched": [PTR, I64, I32, I32, PTR, PTR],
 }
 _RESTYPES = {"blastgpu_status_string": C.c_char_p, "blastgpu_launch_count": C.c_int64,
              "blastgpu_dposv_mixed_workspace_bytes": C.c_size_t}

@@ -209,6 +209,75 @@ def getrs(LU: torch.Tensor, ipiv: torch.Tensor, X: torch.Tensor, info: torch.Ten
     return X
 
 
+LOWER, UPPER = 0, 1
+LEFT, RIGHT = 0, 1
+
+
+def syrk_lower(alpha, A: torch.Tensor, beta, C: torch.Tensor, D: torch.Tensor) -> torch.Tensor:
+    """D_lower = alpha*A*A^T + beta*C_lower (blast::syrkLower, dense/Syrk.hpp:15-145)."""
+    a, c, d = _as_mat(A, "A"), _as_mat(C, "C"), _as_mat(D, "D")
+    m, k = a.rows, a.cols
+    if c.rows != m or c.cols != m or d.rows != m or d.cols != m:
+        raise ValueError("Matrix sizes do not match")
+    for x, nm in ((a, "A"), (c, "C"), (d, "D")):
+        _square_col(x, nm)
+    batch = _batch_of(a, c, d)
+    _lib.call("blastgpu_dsyrk_lower_strided", m, k, float(alpha), a.ptr, a.ld, _bstride(a, batch),
+              float(beta), c.ptr, c.ld, _bstride(c, batch), d.ptr, d.ld, d.bstride, batch, _stream())
+    return D
+
+
+def trsm(uplo: int, unit: bool, A: torch.Tensor, B: torch.Tensor, X: torch.Tensor) -> torch.Tensor:
+    """Solve A*X = B, A triangular (blast::trsm<UpLo, UNIT>(A, B, X), dense/Trsm.hpp:17-66).
+
+    A may be a row-major tensor (BLAST's trans() view of a column-major triangle); X may be B.
+    """
+    a, b, x = _as_mat(A, "A"), _as_mat(B, "B"), _as_mat(X, "X")
+    m, n = b.rows, b.cols
+    if a.rows != m or a.cols != m:
+        raise ValueError("Invalid argument size")
+    if x.rows != m or x.cols != n:
+        raise ValueError("Invalid argument size")
+    _square_col(b, "B")
+    _square_col(x, "X")
+    trans_a = int(a.layout == ROW)
+    batch = _batch_of(a, b, x)
+    _lib.call("blastgpu_dtrsm_strided", int(uplo), trans_a, int(bool(unit)), m, n, a.ptr, a.ld,
+              _bstride(a, batch), b.ptr, b.ld, _bstride(b, batch), x.ptr, x.ld, x.bstride, batch, _stream())
+    return X
+
+
+def trmm(alpha, *args) -> torch.Tensor:
+    """C = alpha*A*B: trmm(alpha, A, uplo, diag, B, C)  (algorithm/Trmm.hpp:260-283), or
+    C = alpha*B*A: trmm(alpha, B, A, uplo, diag, C)  (algorithm/Trmm.hpp:287-310).
+    BLAST implements A upper for the left product and A lower for the right one, non-unit only;
+    the other variants raise NotImplementedError (BLAST: std::logic_error)."""
+    if len(args) != 5:
+        raise TypeError("trmm(alpha, A, uplo, diag, B, C) or trmm(alpha, B, A, uplo, diag, C)")
+    if isinstance(args[1], torch.Tensor):
+        B, A, uplo, diag, C = args
+        side = RIGHT
+    else:
+        A, uplo, diag, B, C = args
+        side = LEFT
+    a, b, c = _as_mat(A, "A"), _as_mat(B, "B"), _as_mat(C, "C")
+    m, n = b.rows, b.cols
+    ka = m if side == LEFT else n
+    if a.rows != ka or a.cols != ka or c.rows != m or c.cols != n:
+        raise ValueError("Matrix sizes do not match")
+    for x, nm in ((a, "A"), (b, "B"), (c, "C")):
+        _square_col(x, nm)
+    batch = _batch_of(a, b, c)
+    st = _lib.lib().blastgpu_dtrmm_strided(side, int(uplo), int(bool(diag)), m, n, float(alpha), a.ptr,
+                                           a.ld, _bstride(a, batch), b.ptr, b.ld, _bstride(b, batch),
+                                           c.ptr, c.ld, c.bstride, batch, _stream())
+    if st == -1001:
+        raise NotImplementedError("trmm variant not implemented (BLAST throws std::logic_error)")
+    if st != 0:
+        raise _lib.BlastGpuError("blastgpu_dtrmm_strided", st)
+    return C
+
+
 def col_major(batch_shape, rows: int, cols: int, device="cuda", ld: int | None = None) -> torch.Tensor:
     """An uninitialised column-major float64 tensor (…, rows, cols) with leading dimension ld."""
     ld = rows if ld is None else ld

@@ -75,6 +75,19 @@ __global__ void fp64_probe_kernel(int iters, double a, double b, double* sink) {
     sink[threadIdx.x] = s;
 }
 
+// The same measurement with one output per thread (no shared sink).
+__global__ void fp64_probe_plain_kernel(double* out, int iters, double a, double b) {
+    double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+    double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; ++i) {
+        x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+        x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+constexpr int kProbeMaxThreads = 160 * 8 * 256;
+__device__ double g_probe_out[kProbeMaxThreads];
 __device__ double g_probe_sink[256];
 
 }  // namespace blastgpu
@@ -144,8 +157,12 @@ int blastgpu_probe_fp64_tflops(double* tflops, blastgpu_stream_t stream) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     double best = 0.0;
-    for (int shape = 0; shape < 4 && e == cudaSuccess; ++shape) {
-        int const chains = shape < 2 ? 8 : 16;
+    double* out = nullptr;
+    e = cudaGetSymbolAddress(reinterpret_cast<void**>(&out), g_probe_out);
+    if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
+    int const nshapes = blocks * threads <= kProbeMaxThreads ? 5 : 4;
+    for (int shape = 0; shape < nshapes && e == cudaSuccess; ++shape) {
+        int const chains = (shape < 2 || shape == 4) ? 8 : 16;
         int const iters = 8192 / chains * 4;
         for (int rep = 0; rep < 3; ++rep) {
             cudaEventRecord(e0, s);
@@ -153,7 +170,8 @@ int blastgpu_probe_fp64_tflops(double* tflops, blastgpu_stream_t stream) {
                 case 0: fp64_probe_kernel<8, 1><<<blocks, threads, 0, s>>>(iters, 0.999, 1e-3, sink); break;
                 case 1: fp64_probe_kernel<8, 4><<<blocks, threads, 0, s>>>(iters, 0.999, 1e-3, sink); break;
                 case 2: fp64_probe_kernel<16, 1><<<blocks, threads, 0, s>>>(iters, 0.999, 1e-3, sink); break;
-                default: fp64_probe_kernel<16, 2><<<blocks, threads, 0, s>>>(iters, 0.999, 1e-3, sink); break;
+                case 3: fp64_probe_kernel<16, 2><<<blocks, threads, 0, s>>>(iters, 0.999, 1e-3, sink); break;
+                default: fp64_probe_plain_kernel<<<blocks, threads, 0, s>>>(out, iters, 0.999, 1e-3); break;
             }
             cudaEventRecord(e1, s);
             e = cudaEventSynchronize(e1);

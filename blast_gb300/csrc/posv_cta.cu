@@ -87,6 +87,7 @@ struct Smem {
 template <typename T, int MAXR>
 __device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf, int* s_info) {
     constexpr int NMAX = 32 * MAXR;
+    __shared__ T rinv[kNB];
     int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) *s_info = 0;
     for (int k0 = 0; k0 < n; k0 += kNB) {
@@ -107,9 +108,9 @@ __device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf,
         for (int kk = 0; kk < k0; kk += kKC) {
             int const kc = min(kKC, k0 - kk);
             __syncthreads();
-            for (int idx = tid; idx < kc * m; idx += kThreads) {
-                int const q = idx / m, r = idx - q * m;
-                buf[q * NMAX + r] = F[(k0 + r) + (int64_t)(kk + q) * ldf];
+            for (int q = 0; q < kc; ++q) {
+                T const* src = F + k0 + (int64_t)(kk + q) * ldf;
+                for (int r = tid; r < m; r += kThreads) buf[q * NMAX + r] = src[r];
             }
             __syncthreads();
             for (int q = 0; q < kc; ++q) {
@@ -140,30 +141,38 @@ __device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf,
             }
         }
         __syncthreads();
-        // Diagonal block: right-looking Cholesky in shared memory.
-        for (int j = 0; j < nb; ++j) {
-            T* cj = buf + j * NMAX;
-            T const d = cj[j];
-            if (!(d > (T)0) && tid == 0 && *s_info == 0) *s_info = k0 + j + 1;
-            T const y = rsqrt_t<T>(d);
-            // column j below the diagonal, inside the block and below it (the panel trsm is
-            // folded into the same right-looking sweep)
-            for (int r = j + 1 + tid; r < m; r += kThreads) cj[r] *= y;
-            __syncthreads();
-            // Every thread has read d by now and nothing below reads cj[j] again.
-            if (tid == 0) cj[j] = d * y;
-            // trailing columns of the panel: buf[l][r] -= buf[j][r] * buf[j][l], r >= l > j
-            int const rest = nb - j - 1;
-            for (int idx = tid; idx < rest * m; idx += kThreads) {
-                int const l = j + 1 + idx / m, r = idx % m;
-                if (r >= l) buf[l * NMAX + r] = fma(-cj[r], cj[l], buf[l * NMAX + r]);
+        // Diagonal block (nb x nb): one warp, lane = row, right-looking, warp barriers only.
+        if (warp == 0) {
+            for (int j = 0; j < nb; ++j) {
+                T const d = buf[j * NMAX + j];
+                if (!(d > (T)0) && lane == 0 && *s_info == 0) *s_info = k0 + j + 1;
+                T const y = rsqrt_t<T>(d);
+                if (lane > j && lane < nb) buf[j * NMAX + lane] *= y;
+                if (lane == 0) { rinv[j] = y; }
+                __syncwarp();
+                if (lane == 0) buf[j * NMAX + j] = d * y;
+                if (lane > j && lane < nb) {
+                    T const lij = buf[j * NMAX + lane];
+                    for (int l = j + 1; l <= lane; ++l)
+                        buf[l * NMAX + lane] = fma(-lij, buf[j * NMAX + l], buf[l * NMAX + lane]);
+                }
+                __syncwarp();
             }
-            __syncthreads();
         }
+        __syncthreads();
+        // Rows below the block: x_j = (p_j - sum_{q<j} x_q l_jq) / l_jj, one thread per row.
+        for (int r = nb + tid; r < m; r += kThreads) {
+            for (int j = 0; j < nb; ++j) {
+                T x = buf[j * NMAX + r];
+                for (int q = 0; q < j; ++q) x = fma(-buf[q * NMAX + r], buf[q * NMAX + j], x);
+                buf[j * NMAX + r] = x * rinv[j];
+            }
+        }
+        __syncthreads();
         // Panel to the factor (lower part).
-        for (int idx = tid; idx < nb * m; idx += kThreads) {
-            int const c = idx / m, r = idx - c * m;
-            if (r >= c) F[(k0 + r) + (int64_t)(k0 + c) * ldf] = buf[c * NMAX + r];
+        for (int c = 0; c < nb; ++c) {
+            T* dst = F + k0 + (int64_t)(k0 + c) * ldf;
+            for (int r = c + tid; r < m; r += kThreads) dst[r] = buf[c * NMAX + r];
         }
         __syncthreads();
     }
@@ -244,16 +253,24 @@ __device__ __forceinline__ double cta_max(double v, double* red) {
 }
 
 // y = A*x for symmetric A given by its lower triangle (binary64); x, y in shared memory.
+// Part 1, y_i = sum_{j<=i} A(i,j) x_j, gives each thread the row pair (p, n-1-p), whose lengths
+// add up to n+1, so all threads do the same work; consecutive threads read consecutive rows of
+// each column. Part 2, y_i += sum_{j>i} A(j,i) x_j, runs a warp down each column.
 __device__ void cta_symv_lower(int n, const double* A, int lda, const double* x, double* y) {
     int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    // y_i = sum_{j<=i} A(i,j) x_j   (thread per row, coalesced down each column)
-    for (int i = tid; i < n; i += kThreads) {
-        double acc = 0.0;
-        for (int j = 0; j <= i; ++j) acc = fma(A[i + (int64_t)j * lda], x[j], acc);
-        y[i] = acc;
+    for (int p = tid; p < (n + 1) / 2; p += kThreads) {
+        int const q = n - 1 - p;
+        double a0 = 0.0, a1 = 0.0;
+        for (int j = 0; j <= p; ++j) {
+            double const xj = x[j];
+            a0 = fma(A[p + (int64_t)j * lda], xj, a0);
+            a1 = fma(A[q + (int64_t)j * lda], xj, a1);
+        }
+        for (int j = p + 1; j <= q; ++j) a1 = fma(A[q + (int64_t)j * lda], x[j], a1);
+        y[p] = a0;
+        if (q != p) y[q] = a1;
     }
     __syncthreads();
-    // y_i += sum_{j>i} A(j,i) x_j   (warp per column, lanes down the column)
     for (int i = warp; i < n; i += kWarps) {
         double acc = 0.0;
         for (int j = i + 1 + lane; j < n; j += 32) acc = fma(A[j + (int64_t)i * lda], x[j], acc);
@@ -320,10 +337,16 @@ __global__ void __launch_bounds__(kThreads, 2) posv_cta_mixed_kernel(Batch batch
     // |A|_inf from the lower triangle: row sums of |A(i,j)| over j<=i plus column sums below.
     double anorm;
     {
-        for (int i = tid; i < n; i += kThreads) {
-            double s = 0.0;
-            for (int j = 0; j <= i; ++j) s += fabs(it.A[i + (int64_t)j * it.lda]);
-            r[i] = s;
+        for (int p = tid; p < (n + 1) / 2; p += kThreads) {
+            int const q = n - 1 - p;
+            double s0 = 0.0, s1 = 0.0;
+            for (int j = 0; j <= p; ++j) {
+                s0 += fabs(it.A[p + (int64_t)j * it.lda]);
+                s1 += fabs(it.A[q + (int64_t)j * it.lda]);
+            }
+            for (int j = p + 1; j <= q; ++j) s1 += fabs(it.A[q + (int64_t)j * it.lda]);
+            r[p] = s0;
+            if (q != p) r[q] = s1;
         }
         __syncthreads();
         int const lane = tid & 31, warp = tid >> 5;
@@ -355,22 +378,23 @@ __global__ void __launch_bounds__(kThreads, 2) posv_cta_mixed_kernel(Batch batch
         if (info == 0) cta_potrs<float, MAXR>(n, F, n, w);
         for (int i = tid; i < n; i += kThreads) x[i] = info == 0 ? (double)w[i] : CUDART_NAN;
         __syncthreads();
-        double be = CUDART_INF;
+        double be = CUDART_NAN;  // a failed binary32 factorisation leaves no solution to refine
         int it_count = 0;
-        for (;;) {
+        while (info == 0) {
             // r = b - A x (binary64)
             cta_symv_lower(n, it.A, it.lda, x, r);
             double rm = 0.0, xm = 0.0;
             for (int i = tid; i < n; i += kThreads) {
                 r[i] = bb[i] - r[i];
-                rm = fmax(rm, fabs(r[i]));
-                xm = fmax(xm, fabs(x[i]));
+                double const ar = fabs(r[i]), ax = fabs(x[i]);
+                rm = (ar > rm || ar != ar) ? ar : rm;  // NaN-propagating maxima
+                xm = (ax > xm || ax != ax) ? ax : xm;
             }
             rm = cta_max(rm, red);
             xm = cta_max(xm, red);
             double const den = anorm * xm + bnorm;
             be = den > 0.0 ? rm / den : (rm == 0.0 ? 0.0 : CUDART_INF);
-            if (!(be > args.tol) || it_count >= args.max_iter || info != 0) break;
+            if (!(be > args.tol) || it_count >= args.max_iter) break;
             // d = F^{-T} F^{-1} (r / s) * s in binary32, with s = |r|_inf keeping r in range
             double const s = rm;
             for (int i = tid; i < n; i += kThreads) w[i] = (float)(r[i] / s);
@@ -389,6 +413,75 @@ __global__ void __launch_bounds__(kThreads, 2) posv_cta_mixed_kernel(Batch batch
         if (args.iters) args.iters[b] = total_iters;
         if (args.berr) args.berr[b] = worst;
     }
+}
+
+// Adjoint of X = A^{-1} B for SPD A (no BLAST counterpart): given the factor L (or A, to
+// recompute it) and dl/dX, writes dl/dB = A^{-1} dl/dX and the symmetric
+// dl/dA = -(dl/dB X^T + X dl/dB^T)/2, all binary64.
+struct BwdItem {
+    int n, nrhs;
+    const double* A; int lda;
+    double* L; int ldl;
+    const double* X; int ldx;
+    const double* G; int ldg;   // dl/dX
+    double* GB; int ldgb;       // dl/dB
+    double* GA; int ldga;       // dl/dA
+};
+
+struct DescBwd {
+    const blastgpu_posv_bwd_desc* desc;
+    __device__ BwdItem get(int64_t b) const {
+        blastgpu_posv_bwd_desc const& d = desc[b];
+        return {d.A.rows, d.X.cols, d.A.data, d.A.ld, d.L.data, d.L.ld, d.X.data, d.X.ld,
+                d.Xbar.data, d.Xbar.ld, d.Bbar.data, d.Bbar.ld, d.Abar.data, d.Abar.ld};
+    }
+};
+
+template <int MAXR, class Batch>
+__global__ void __launch_bounds__(kThreads, 1) posv_bwd_kernel(Batch batch, int64_t count, int recompute,
+                                                               int32_t* info) {
+    using S = Smem<double, MAXR>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double* buf = reinterpret_cast<double*>(smem_raw);
+    double* vec = buf + S::kBufElems;
+    __shared__ int s_info;
+    int64_t const b = blockIdx.x;
+    if (b >= count) return;
+    BwdItem const it = batch.get(b);
+    int const n = it.n, tid = threadIdx.x;
+    if (recompute) {
+        int const r = cta_potrf<double, MAXR>(n, it.A, it.lda, it.L, it.ldl, buf, &s_info);
+        if (tid == 0 && info) info[b] = r;
+    } else if (tid == 0 && info) {
+        info[b] = 0;
+    }
+    __syncthreads();
+    for (int c = 0; c < it.nrhs; ++c) {
+        for (int i = tid; i < n; i += kThreads) vec[i] = it.G[i + (int64_t)c * it.ldg];
+        __syncthreads();
+        cta_potrs<double, MAXR>(n, it.L, it.ldl, vec);
+        for (int i = tid; i < n; i += kThreads) it.GB[i + (int64_t)c * it.ldgb] = vec[i];
+        __syncthreads();
+    }
+    for (int e = tid; e < n * n; e += kThreads) {
+        int const i = e % n, j = e / n;
+        double acc = 0.0;
+        for (int c = 0; c < it.nrhs; ++c) {
+            acc = fma(it.GB[i + (int64_t)c * it.ldgb], it.X[j + (int64_t)c * it.ldx], acc);
+            acc = fma(it.X[i + (int64_t)c * it.ldx], it.GB[j + (int64_t)c * it.ldgb], acc);
+        }
+        it.GA[i + (int64_t)j * it.ldga] = -0.5 * acc;
+    }
+}
+
+template <int MAXR>
+int launch_bwd(DescBwd const& batch, int64_t count, int recompute, int32_t* info, cudaStream_t s) {
+    size_t const smem = Smem<double, MAXR>::kBytes;
+    cudaError_t e = cudaFuncSetAttribute(posv_bwd_kernel<MAXR, DescBwd>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
+    posv_bwd_kernel<MAXR, DescBwd><<<(unsigned)count, kThreads, smem, s>>>(batch, count, recompute, info);
+    return check_launch();
 }
 
 template <int MAXR, class Batch>
@@ -454,6 +547,23 @@ int blastgpu_dposv_mixed_batched(const blastgpu_posv_desc* desc, int64_t batch, 
     if (max_iter < 0) return -6;
     CtaArgs a{batch, info, iters, berr, tol, max_iter};
     return dispatch_cta(true, max_n, DescPosv{desc, static_cast<char*>(workspace)}, a, as_cuda(stream));
+}
+
+int blastgpu_dposv_bwd_batched(const blastgpu_posv_bwd_desc* desc, int64_t batch, int max_n,
+                               int recompute, int32_t* info, blastgpu_stream_t stream) {
+    if (batch < 0) return -2;
+    if (batch == 0) return BLASTGPU_SUCCESS;
+    if (!desc) return -1;
+    if (max_n < 0) return -3;
+    if (recompute != 0 && recompute != 1) return -4;
+    if (batch > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
+    DescBwd d{desc};
+    cudaStream_t const s = as_cuda(stream);
+    if (max_n <= 64) return launch_bwd<2>(d, batch, recompute, info, s);
+    if (max_n <= 128) return launch_bwd<4>(d, batch, recompute, info, s);
+    if (max_n <= 256) return launch_bwd<8>(d, batch, recompute, info, s);
+    if (max_n <= 512) return launch_bwd<16>(d, batch, recompute, info, s);
+    return BLASTGPU_ERR_TOO_LARGE;
 }
 
 }  // extern "C"

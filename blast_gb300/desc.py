@@ -24,6 +24,10 @@ POSV_DTYPE = np.dtype([("A", MAT_DTYPE), ("L", MAT_DTYPE), ("B", MAT_DTYPE), ("X
                        ("ws_offset", "<i8")], align=True)
 assert POSV_DTYPE.itemsize == 136
 
+POSV_BWD_DTYPE = np.dtype([("A", MAT_DTYPE), ("L", MAT_DTYPE), ("X", MAT_DTYPE),
+                           ("Xbar", MAT_DTYPE), ("Bbar", MAT_DTYPE), ("Abar", MAT_DTYPE)], align=True)
+assert POSV_BWD_DTYPE.itemsize == 192
+
 EMPTY_MAT = (0, 0, 0, 1, 0, 0, 0)
 
 

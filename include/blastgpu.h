@@ -117,6 +117,33 @@ int blastgpu_dgemm_batched(const blastgpu_gemm_desc* desc, int64_t batch, int ma
                            int max_k, blastgpu_stream_t stream);
 
 /* ---------------------------------------------------------------------------------------------
+ * syrkLower: D_lower = alpha*A*A^T + beta*C_lower, A m x k, C and D m x m, column-major; only
+ * the lower triangle of C is read and of D written. Replaces blast::syrkLower(alpha, A, beta, C, D)
+ * (dense/Syrk.hpp:15-145); bit-identical to its order of operations. D may equal C.
+ * ------------------------------------------------------------------------------------------- */
+int blastgpu_dsyrk_lower_strided(int m, int k, double alpha, const double* A, int lda, int64_t stride_a,
+                                 double beta, const double* C, int ldc, int64_t stride_c, double* D,
+                                 int ldd, int64_t stride_d, int64_t batch, blastgpu_stream_t stream);
+
+/* trsm: solves op(A)*X = B for X, A m x m triangular (uplo), op(A) = A or A^T (trans_a), unit
+ * diagonal if unit = 1, B and X m x n column-major; X may equal B. Replaces
+ * blast::trsm<UpLo, UNIT>(A, B, X) (dense/Trsm.hpp:17-66), with trans_a covering BLAST's trans()
+ * view of A; bit-identical to BLAST's scalar substitution (IEEE division by the diagonal). */
+int blastgpu_dtrsm_strided(int uplo, int trans_a, int unit, int m, int n, const double* A, int lda,
+                           int64_t stride_a, const double* B, int ldb, int64_t stride_b, double* X,
+                           int ldx, int64_t stride_x, int64_t batch, blastgpu_stream_t stream);
+
+/* trmm: C = alpha*A*B (side = LEFT, A m x m upper) or C = alpha*B*A (side = RIGHT, A n x n lower),
+ * B and C m x n column-major; C must not overlap A or B. Replaces blast::trmm(alpha, A, uplo, diag,
+ * B, C) and blast::trmm(alpha, B, A, uplo, diag, C) (algorithm/Trmm.hpp:260-310). As in BLAST, the
+ * other (side, uplo) pairs and unit diagonals are not implemented: BLASTGPU_ERR_NOT_IMPLEMENTED
+ * (BLAST throws std::logic_error, algorithm/Trmm.hpp:101-124, 240). Only the named triangle of A
+ * is read. */
+int blastgpu_dtrmm_strided(int side, int uplo, int unit, int m, int n, double alpha, const double* A,
+                           int lda, int64_t stride_a, const double* B, int ldb, int64_t stride_b,
+                           double* C, int ldc, int64_t stride_c, int64_t batch, blastgpu_stream_t stream);
+
+/* ---------------------------------------------------------------------------------------------
  * potrf: lower Cholesky factor L of a symmetric positive definite n x n A (only the lower
  * triangle of A is read; the strict upper triangle of L is not written). L may equal A.
  * Replaces blast::potrf(A, L) dense (dense/Potrf.hpp:66-106) and panel (panel/Potrf.hpp:59-106).
@@ -205,6 +232,24 @@ size_t blastgpu_dposv_mixed_workspace_bytes(int n);
 int blastgpu_dposv_mixed_batched(const blastgpu_posv_desc* desc, int64_t batch, int max_n,
                                  void* workspace, double tol, int max_iter, int32_t* info,
                                  int32_t* iters, double* berr, blastgpu_stream_t stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Adjoints (no BLAST counterpart). For X = A^{-1} B with A SPD and a scalar loss l:
+ *   dl/dB = A^{-1} dl/dX,   dl/dA = -(dl/dB X^T + X dl/dB^T) / 2  (symmetrised),
+ * from the forward factor L (recompute = 0), or recomputing L from A into the L matrix
+ * (recompute = 1, e.g. in caller workspace) when the forward factor was not kept.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct blastgpu_posv_bwd_desc {
+    blastgpu_mat A;     /* n x n SPD input (read only when recompute = 1) */
+    blastgpu_mat L;     /* n x n factor: input, or output when recompute = 1 */
+    blastgpu_mat X;     /* n x nrhs forward solution */
+    blastgpu_mat Xbar;  /* n x nrhs incoming gradient dl/dX */
+    blastgpu_mat Bbar;  /* n x nrhs output dl/dB */
+    blastgpu_mat Abar;  /* n x n output dl/dA (full symmetric matrix written) */
+} blastgpu_posv_bwd_desc; /* 192 bytes */
+
+int blastgpu_dposv_bwd_batched(const blastgpu_posv_bwd_desc* desc, int64_t batch, int max_n,
+                               int recompute, int32_t* info, blastgpu_stream_t stream);
 
 #ifdef __cplusplus
 }

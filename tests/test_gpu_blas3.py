@@ -1,0 +1,119 @@
+"""GPU parity of batched syrkLower, trsm and trmm against the oracle (bit for bit), over the
+reference's own size sweeps (dense/SyrkTest.cpp, TrsmTest.cpp, TrmmTest.cpp)."""
+import numpy as np
+import pytest
+
+from helpers import approx_equal, to_dev
+
+pytestmark = pytest.mark.gpu
+
+
+def F(a):
+    return np.asfortranarray(a)
+
+
+def test_syrk_lower_sweep_bitexact(gpu, oracle_lib):
+    import torch
+
+    rng = np.random.default_rng(1)
+    for m in (1, 2, 5, 12, 13, 20, 33):
+        for k in (1, 4, 20, 31):
+            batch = 3
+            A = rng.random((batch, m, k))
+            C = rng.random((batch, m, m))
+            C = C + np.swapaxes(C, 1, 2)
+            alpha, beta = 0.75, -1.25
+            dA, dC = to_dev(A), to_dev(C)
+            dD = to_dev(np.full((batch, m, m), 3.0))
+            gpu.syrk_lower(alpha, dA, beta, dC, dD)
+            torch.cuda.synchronize()
+            D = dD.cpu().numpy()
+            for b in range(batch):
+                Dr = F(np.full((m, m), 3.0))
+                oracle_lib.syrk_lower(alpha, F(A[b]), beta, F(C[b]), Dr)
+                assert np.array_equal(D[b], Dr), (m, k)  # upper triangle untouched too
+
+
+@pytest.mark.parametrize("uplo,unit", [(0, 0), (0, 1), (1, 0), (1, 1)])
+def test_trsm_sweep_bitexact(gpu, oracle_lib, uplo, unit):
+    import torch
+
+    rng = np.random.default_rng(10 + 2 * uplo + unit)
+    for m in (1, 4, 9, 17, 50):
+        for n in (1, 3, 8, 50):
+            batch = 4
+            A = rng.random((batch, m, m)) + np.eye(m)
+            B = rng.random((batch, m, n))
+            dA, dB = to_dev(A), to_dev(B)
+            dX = gpu.col_major((batch,), m, n, "cuda")
+            gpu.trsm(uplo, unit, dA, dB, dX)
+            gpu.trsm(uplo, unit, dA, dB, dB)  # X aliasing B
+            torch.cuda.synchronize()
+            X, Xa = dX.cpu().numpy(), dB.cpu().numpy()
+            for b in range(batch):
+                Xr = F(np.zeros((m, n)))
+                oracle_lib.trsm(uplo, unit, F(A[b]), F(B[b]), Xr)
+                assert np.array_equal(X[b], Xr), (m, n)
+                assert np.array_equal(Xa[b], Xr), (m, n)
+                At = np.tril(A[b]) if uplo == 0 else np.triu(A[b])
+                if unit:
+                    np.fill_diagonal(At, 1.0)
+                assert approx_equal(At @ X[b], B[b], 1e-10, 1e-10)
+
+
+def test_trsm_transposed_view(gpu, oracle_lib):
+    """trsm<Upper>(trans(L), Y, X): A given as a row-major tensor (BLAST's trans() view)."""
+    import torch
+
+    rng = np.random.default_rng(4)
+    m, n, batch = 23, 5, 3
+    Lh = np.tril(rng.random((batch, m, m))) + np.eye(m)
+    Y = rng.random((batch, m, n))
+    dL = to_dev(Lh)
+    dX = to_dev(Y)
+    gpu.trsm(1, 0, dL.mT, dX, dX)
+    torch.cuda.synchronize()
+    X = dX.cpu().numpy()
+    for b in range(batch):
+        Xr = F(Y[b].copy())
+        oracle_lib.trsm(1, 0, F(Lh[b]), Xr, Xr, trans_a=1)
+        assert np.array_equal(X[b], Xr)
+
+
+def test_trmm_sweep_bitexact(gpu, oracle_lib):
+    import torch
+
+    rng = np.random.default_rng(5)
+    for m in (1, 3, 8, 13, 20):
+        for n in (1, 4, 7, 20):
+            batch = 2
+            alpha = 0.625
+            A = rng.random((batch, m, m))  # strictly lower part non-zero: must not be read
+            B = rng.random((batch, m, n))
+            dC = gpu.col_major((batch,), m, n, "cuda")
+            gpu.trmm(alpha, to_dev(A), gpu.UPPER, False, to_dev(B), dC)
+            A2 = rng.random((batch, n, n))
+            B2 = rng.random((batch, m, n))
+            dC2 = gpu.col_major((batch,), m, n, "cuda")
+            gpu.trmm(alpha, to_dev(B2), to_dev(A2), gpu.LOWER, False, dC2)
+            torch.cuda.synchronize()
+            C, C2 = dC.cpu().numpy(), dC2.cpu().numpy()
+            for b in range(batch):
+                Cr = F(np.zeros((m, n)))
+                assert oracle_lib.trmm(0, 1, 0, alpha, F(A[b]), F(B[b]), Cr) == 0
+                assert np.array_equal(C[b], Cr)
+                Cr2 = F(np.zeros((m, n)))
+                assert oracle_lib.trmm(1, 0, 0, alpha, F(A2[b]), F(B2[b]), Cr2) == 0
+                assert np.array_equal(C2[b], Cr2)
+
+
+def test_trmm_unimplemented_variants(gpu):
+    dA = to_dev(np.eye(3)[None])
+    dB = to_dev(np.ones((1, 3, 3)))
+    dC = gpu.col_major((1,), 3, 3, "cuda")
+    with pytest.raises(NotImplementedError):
+        gpu.trmm(1.0, dA, gpu.LOWER, False, dB, dC)
+    with pytest.raises(NotImplementedError):
+        gpu.trmm(1.0, dB, dA, gpu.UPPER, False, dC)
+    with pytest.raises(NotImplementedError):
+        gpu.trmm(1.0, dA, gpu.UPPER, True, dB, dC)
