@@ -123,7 +123,7 @@ def peak_fp64_tflops() -> float:
     return out.value
 
 
-def make_mixed_inputs(count: int, seed: int, device):
+def make_mixed_inputs(count: int, seed: int, device, gen: str = "qr"):
     """The mixed-precision workload: n ~ U{64..512}; A = Q diag(lambda) Q^T with Q from the QR of a
     seeded Gaussian and lambda log-spaced so that cond(A) is 1e2, 1e4 or 1e6 (a third each);
     one N(0,1) right-hand side. Built on the device in binary64, grouped by size."""
@@ -142,6 +142,12 @@ def make_mixed_inputs(count: int, seed: int, device):
     for n in np.unique(ns):
         idx = np.nonzero(ns == n)[0]
         G = torch.randn(len(idx), n, n, generator=g, device=device, dtype=torch.float64)
+        if gen == "gram":
+            # Profiling stand-in without torch.linalg (SPD, same sizes, well conditioned).
+            M = G @ G.mT / n + torch.eye(n, device=device, dtype=torch.float64)
+            for j, i in enumerate(idx):
+                A.view(int(i)).copy_(M[j])
+            continue
         Q, _ = torch.linalg.qr(G)
         lam = torch.stack([torch.logspace(0, -float(np.log10(conds[i])), n, device=device,
                                           dtype=torch.float64) for i in idx])
@@ -154,7 +160,7 @@ def make_mixed_inputs(count: int, seed: int, device):
     return ns, conds, A, B
 
 
-def mixed_ir_comparison(steps: int, count: int = 8192):
+def mixed_ir_comparison(steps: int, count: int = 8192, gen: str = "qr"):
     """FP64 vs mixed-precision + refinement on the ragged n in [64, 512] batch (one CTA per
     matrix, one launch per step for each path)."""
     import numpy as np
@@ -163,7 +169,7 @@ def mixed_ir_comparison(steps: int, count: int = 8192):
     from blast_gb300.ragged import Packed, PosvPlan
 
     dev = torch.device("cuda", torch.cuda.current_device())
-    ns, conds, A, B = make_mixed_inputs(count, 4321, dev)
+    ns, conds, A, B = make_mixed_inputs(count, 4321, dev, gen)
     ones = np.ones_like(ns)
     X64, X32 = Packed(ns, ones, dev), Packed(ns, ones, dev)
     L = Packed(ns, ns, dev)
@@ -199,7 +205,8 @@ def mixed_ir_comparison(steps: int, count: int = 8192):
     out["fp64"]["info_nonzero"] = int(np.sum(info64 != 0))
     out["speedup_matrices_per_s"] = out["mixed"]["matrices_per_s"] / out["fp64"]["matrices_per_s"]
     out["workload"] = (f"{count} SPD matrices, n ~ U{{64..512}}, A = Q diag(lambda) Q^T, "
-                       "cond in {1e2,1e4,1e6}, 1 RHS; tol 1e-12")
+                       "cond in {1e2,1e4,1e6}, 1 RHS; tol 1e-12" if gen == "qr" else
+                       f"{count} SPD matrices, n ~ U{{64..512}}, A = G G^T/n + I (profiling)")
     return out
 
 
@@ -392,6 +399,14 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_mixed_only(args):
+    """Only the FP64-vs-mixed comparison (profiling runs on a smaller ragged batch)."""
+    import torch
+
+    torch.cuda.set_device(0)
+    print(json.dumps(mixed_ir_comparison(max(1, args.steps), args.mixed_count, args.mixed_gen)), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -404,8 +419,16 @@ def main():
     ap.add_argument("--batch", type=int, default=BATCH, help="matrices per GPU (default 50,000)")
     ap.add_argument("--no-mixed", action="store_true",
                     help="skip the FP64-vs-mixed comparison on the ragged n in [64, 512] batch")
+    ap.add_argument("--only-mixed", action="store_true",
+                    help="run only the FP64-vs-mixed comparison (with --mixed-count matrices)")
+    ap.add_argument("--mixed-count", type=int, default=8192)
+    ap.add_argument("--mixed-gen", choices=["qr", "gram"], default="qr",
+                    help="qr: the workload's Q diag(lambda) Q^T matrices; gram: G G^T/n + I, for "
+                         "profilers under which torch.linalg cannot load")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.only_mixed:
+        run_mixed_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -79,8 +79,35 @@ struct Smem {
     static constexpr int kPanelElems = kNB * NMAX;
     static constexpr int kStageElems = kKC * NMAX;
     static constexpr int kBufElems = kPanelElems > kStageElems ? kPanelElems : kStageElems;
-    static constexpr size_t kBytes = sizeof(T) * kBufElems + sizeof(double) * (4 * NMAX + 64);
+    static constexpr int kBlkElems = 32 * 33;  // one padded 32 x 32 diagonal block
+    static constexpr size_t kBytes =
+        sizeof(T) * (kBufElems + kBlkElems) + sizeof(double) * (4 * NMAX + 64);
 };
+
+// Cholesky of the nb x nb diagonal block held in registers, lane = row (a[k] = block(lane, k)),
+// fully unrolled: step j takes the pivot from lane j, scales column j, and updates the trailing
+// lower part with column j fetched from the owning lanes by shuffles. rdiag receives 1/l_jj on
+// lane j. Returns (on every lane) the first bad pivot + 1 within the block, or 0.
+template <typename T>
+__device__ __forceinline__ int warp_chol32(T (&a)[32], int nb, int lane, T& rdiag) {
+    int bad = 0;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        if (j < nb) {
+            T const d = __shfl_sync(0xffffffffu, a[j], j);
+            if (!(d > (T)0) && bad == 0) bad = j + 1;
+            T const y = rsqrt_t<T>(d);
+            if (lane == j) { rdiag = y; a[j] = d * y; }
+            else if (lane > j) a[j] *= y;
+#pragma unroll
+            for (int l = j + 1; l < 32; ++l) {
+                T const llj = __shfl_sync(0xffffffffu, a[j], l);
+                if (lane >= l && l < nb) a[l] = fma(-a[j], llj, a[l]);
+            }
+        }
+    }
+    return bad;
+}
 
 // Left-looking blocked Cholesky of the n x n matrix: lower(A) -> F (precision T, ld ldf).
 // Returns info (0 or first bad pivot + 1) identically in all threads.
@@ -141,31 +168,35 @@ __device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf,
             }
         }
         __syncthreads();
-        // Diagonal block (nb x nb): one warp, lane = row, right-looking, warp barriers only.
+        // Diagonal block (nb x nb): one warp, in registers (lane = row).
         if (warp == 0) {
-            for (int j = 0; j < nb; ++j) {
-                T const d = buf[j * NMAX + j];
-                if (!(d > (T)0) && lane == 0 && *s_info == 0) *s_info = k0 + j + 1;
-                T const y = rsqrt_t<T>(d);
-                if (lane > j && lane < nb) buf[j * NMAX + lane] *= y;
-                if (lane == 0) { rinv[j] = y; }
-                __syncwarp();
-                if (lane == 0) buf[j * NMAX + j] = d * y;
-                if (lane > j && lane < nb) {
-                    T const lij = buf[j * NMAX + lane];
-                    for (int l = j + 1; l <= lane; ++l)
-                        buf[l * NMAX + lane] = fma(-lij, buf[j * NMAX + l], buf[l * NMAX + lane]);
-                }
-                __syncwarp();
+            T a[32];
+#pragma unroll
+            for (int k = 0; k < 32; ++k) a[k] = (k < nb && lane < nb) ? buf[k * NMAX + lane] : (T)0;
+            T rd = (T)0;
+            int const bad = warp_chol32<T>(a, nb, lane, rd);
+            if (bad && lane == 0 && *s_info == 0) *s_info = k0 + bad;
+            if (lane < nb) {
+#pragma unroll
+                for (int k = 0; k < 32; ++k)
+                    if (k <= lane) buf[k * NMAX + lane] = a[k];
+                rinv[lane] = rd;
             }
         }
         __syncthreads();
-        // Rows below the block: x_j = (p_j - sum_{q<j} x_q l_jq) / l_jj, one thread per row.
+        // Rows below the block: x_j = (p_j - sum_{q<j} x_q l_jq) / l_jj, one thread per row, the
+        // row in registers and the block's entries broadcast from shared memory.
         for (int r = nb + tid; r < m; r += kThreads) {
-            for (int j = 0; j < nb; ++j) {
-                T x = buf[j * NMAX + r];
-                for (int q = 0; q < j; ++q) x = fma(-buf[q * NMAX + r], buf[q * NMAX + j], x);
-                buf[j * NMAX + r] = x * rinv[j];
+            T x[32];
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                if (j < nb) {
+                    T v = buf[j * NMAX + r];
+#pragma unroll
+                    for (int q = 0; q < j; ++q) v = fma(-x[q], buf[q * NMAX + j], v);
+                    x[j] = v * rinv[j];
+                    buf[j * NMAX + r] = x[j];
+                }
             }
         }
         __syncthreads();
@@ -179,28 +210,47 @@ __device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf,
     return *s_info;
 }
 
+// Stages the nb x nb diagonal block at (j0, j0) of F into blk (column-major, stride 33), with
+// an identity completion outside nb.
+template <typename T>
+__device__ __forceinline__ void stage_block(const T* F, int ldf, int j0, int nb, T* blk) {
+    for (int idx = threadIdx.x; idx < 32 * 32; idx += kThreads) {
+        int const r = idx & 31, c = idx >> 5;
+        blk[c * 33 + r] = (r < nb && c < nb) ? F[(j0 + r) + (int64_t)(j0 + c) * ldf] : (T)(r == c ? 1 : 0);
+    }
+}
+
 // In-place solve with the factor: v := F^{-T} F^{-1} v (v in shared memory, precision T).
+// Each 32 x 32 diagonal block is solved by one warp from registers (rows for the forward pass,
+// columns for the backward pass), fully unrolled; the other rows are updated by all threads.
 template <typename T, int MAXR>
-__device__ void cta_potrs(int n, const T* F, int ldf, T* v) {
+__device__ void cta_potrs(int n, const T* F, int ldf, T* v, T* blk) {
     int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // forward: F * y = v
     for (int j0 = 0; j0 < n; j0 += 32) {
         int const nb = min(32, n - j0);
+        stage_block<T>(F, ldf, j0, nb, blk);
+        __syncthreads();
         if (warp == 0) {
+            T a[32];
+#pragma unroll
+            for (int k = 0; k < 32; ++k) a[k] = blk[k * 33 + lane];
+            T const rd = rcp_t<T>(blk[lane * 33 + lane]);
             T x = lane < nb ? v[j0 + lane] : (T)0;
-            for (int j = 0; j < nb; ++j) {
-                T const fjj = F[(j0 + j) + (int64_t)(j0 + j) * ldf];
-                T xj = __shfl_sync(0xffffffffu, x, j);
-                xj = xj * rcp_t<T>(fjj);
-                if (lane == j) x = xj;
-                if (lane > j && lane < nb) x = fma(-F[(j0 + lane) + (int64_t)(j0 + j) * ldf], xj, x);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                if (lane == j) x *= rd;
+                T const xj = __shfl_sync(0xffffffffu, x, j);
+                if (lane > j) x = fma(-a[j], xj, x);
             }
             if (lane < nb) v[j0 + lane] = x;
         }
         __syncthreads();
         for (int r = j0 + nb + tid; r < n; r += kThreads) {
             T acc = v[r];
-            for (int j = 0; j < nb; ++j) acc = fma(-F[r + (int64_t)(j0 + j) * ldf], v[j0 + j], acc);
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                if (j < nb) acc = fma(-F[r + (int64_t)(j0 + j) * ldf], v[j0 + j], acc);
             v[r] = acc;
         }
         __syncthreads();
@@ -209,9 +259,8 @@ __device__ void cta_potrs(int n, const T* F, int ldf, T* v) {
     int const last = ((n - 1) / 32) * 32;
     for (int j0 = last; j0 >= 0; j0 -= 32) {
         int const nb = min(32, n - j0);
-        // rows of this block get the contributions of the rows below it: v_i -= sum_r F(r,i) v_r
+        // rows of this block take the contributions of the rows below: v_i -= sum_r F(r,i) v_r
         if (j0 + nb < n) {
-            // each warp takes columns i of the block; lanes split r with a shuffle reduction
             for (int i = warp; i < nb; i += kWarps) {
                 T acc = (T)0;
                 for (int r = j0 + nb + lane; r < n; r += 32) acc = fma(F[r + (int64_t)(j0 + i) * ldf], v[r], acc);
@@ -219,16 +268,20 @@ __device__ void cta_potrs(int n, const T* F, int ldf, T* v) {
                 for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
                 if (lane == 0) v[j0 + i] -= acc;
             }
-            __syncthreads();
         }
+        stage_block<T>(F, ldf, j0, nb, blk);
+        __syncthreads();
         if (warp == 0) {
+            T c[32];
+#pragma unroll
+            for (int k = 0; k < 32; ++k) c[k] = blk[lane * 33 + k];  // column lane: F(k, lane)
+            T const rd = rcp_t<T>(blk[lane * 33 + lane]);
             T x = lane < nb ? v[j0 + lane] : (T)0;
-            for (int j = nb - 1; j >= 0; --j) {
-                T const fjj = F[(j0 + j) + (int64_t)(j0 + j) * ldf];
-                T xj = __shfl_sync(0xffffffffu, x, j);
-                xj = xj * rcp_t<T>(fjj);
-                if (lane == j) x = xj;
-                if (lane < j) x = fma(-F[(j0 + j) + (int64_t)(j0 + lane) * ldf], xj, x);
+#pragma unroll
+            for (int j = 31; j >= 0; --j) {
+                if (lane == j) x *= rd;
+                T const xj = __shfl_sync(0xffffffffu, x, j);
+                if (lane < j) x = fma(-c[j], xj, x);
             }
             if (lane < nb) v[j0 + lane] = x;
         }
@@ -296,7 +349,8 @@ __global__ void __launch_bounds__(kThreads, 1) posv_cta_f64_kernel(Batch batch, 
     using S = Smem<double, MAXR>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double* buf = reinterpret_cast<double*>(smem_raw);
-    double* vec = buf + S::kBufElems;
+    double* blk = buf + S::kBufElems;
+    double* vec = blk + S::kBlkElems;
     __shared__ int s_info;
     int64_t const b = blockIdx.x;
     if (b >= args.batch) return;
@@ -307,7 +361,7 @@ __global__ void __launch_bounds__(kThreads, 1) posv_cta_f64_kernel(Batch batch, 
     for (int c = 0; c < it.nrhs; ++c) {
         for (int i = threadIdx.x; i < n; i += kThreads) vec[i] = it.B[i + (int64_t)c * it.ldb];
         __syncthreads();
-        cta_potrs<double, MAXR>(n, it.L, it.ldl, vec);
+        cta_potrs<double, MAXR>(n, it.L, it.ldl, vec, blk);
         for (int i = threadIdx.x; i < n; i += kThreads) it.X[i + (int64_t)c * it.ldx] = vec[i];
         __syncthreads();
     }
@@ -320,7 +374,8 @@ __global__ void __launch_bounds__(kThreads, 2) posv_cta_mixed_kernel(Batch batch
     constexpr int NMAX = S::NMAX;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* buf = reinterpret_cast<float*>(smem_raw);
-    double* x = reinterpret_cast<double*>(smem_raw + sizeof(float) * S::kBufElems);
+    float* blk = buf + S::kBufElems;
+    double* x = reinterpret_cast<double*>(smem_raw + sizeof(float) * (S::kBufElems + S::kBlkElems));
     double* r = x + NMAX;
     double* bb = r + NMAX;
     float* w = reinterpret_cast<float*>(bb + NMAX);  // NMAX floats (fits in the 4th vector)
@@ -375,7 +430,7 @@ __global__ void __launch_bounds__(kThreads, 2) posv_cta_mixed_kernel(Batch batch
         // x0 = F^{-T} F^{-1} b in binary32
         for (int i = tid; i < n; i += kThreads) w[i] = (float)bb[i];
         __syncthreads();
-        if (info == 0) cta_potrs<float, MAXR>(n, F, n, w);
+        if (info == 0) cta_potrs<float, MAXR>(n, F, n, w, blk);
         for (int i = tid; i < n; i += kThreads) x[i] = info == 0 ? (double)w[i] : CUDART_NAN;
         __syncthreads();
         double be = CUDART_NAN;  // a failed binary32 factorisation leaves no solution to refine
@@ -399,7 +454,7 @@ __global__ void __launch_bounds__(kThreads, 2) posv_cta_mixed_kernel(Batch batch
             double const s = rm;
             for (int i = tid; i < n; i += kThreads) w[i] = (float)(r[i] / s);
             __syncthreads();
-            cta_potrs<float, MAXR>(n, F, n, w);
+            cta_potrs<float, MAXR>(n, F, n, w, blk);
             for (int i = tid; i < n; i += kThreads) x[i] += (double)w[i] * s;
             __syncthreads();
             ++it_count;
@@ -443,7 +498,8 @@ __global__ void __launch_bounds__(kThreads, 1) posv_bwd_kernel(Batch batch, int6
     using S = Smem<double, MAXR>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double* buf = reinterpret_cast<double*>(smem_raw);
-    double* vec = buf + S::kBufElems;
+    double* blk = buf + S::kBufElems;
+    double* vec = blk + S::kBlkElems;
     __shared__ int s_info;
     int64_t const b = blockIdx.x;
     if (b >= count) return;
@@ -459,7 +515,7 @@ __global__ void __launch_bounds__(kThreads, 1) posv_bwd_kernel(Batch batch, int6
     for (int c = 0; c < it.nrhs; ++c) {
         for (int i = tid; i < n; i += kThreads) vec[i] = it.G[i + (int64_t)c * it.ldg];
         __syncthreads();
-        cta_potrs<double, MAXR>(n, it.L, it.ldl, vec);
+        cta_potrs<double, MAXR>(n, it.L, it.ldl, vec, blk);
         for (int i = tid; i < n; i += kThreads) it.GB[i + (int64_t)c * it.ldgb] = vec[i];
         __syncthreads();
     }
