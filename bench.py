@@ -321,30 +321,27 @@ def run_ours(args):
         print(json.dumps({"ms_per_step": ms, "value": ws * BATCH / (ms * 1e-3), "batch": BATCH}))
         return
 
-    # End to end through the public API: pinned host A, B -> device -> posv -> L, X to host.
-    hA = torch.empty(A.mT.shape, dtype=torch.float64, pin_memory=True)
-    hB = torch.empty(B.mT.shape, dtype=torch.float64, pin_memory=True)
-    hA.copy_(A.mT)
-    hB.copy_(B.mT)
-    hL = torch.empty_like(hA, pin_memory=True)
-    hX = torch.empty_like(hB, pin_memory=True)
-    dA, dB = A, B
+    # End to end through the public host-buffer API: pinned host A, B -> device -> posv -> L, X
+    # back to pinned host memory, every step, in chunks pipelined over three streams.
+    from blast_gb300.host import PosvHostPipeline, pinned_col_major
 
-    def e2e_step():
-        dA.mT.copy_(hA, non_blocking=True)
-        dB.mT.copy_(hB, non_blocking=True)
-        bg.posv(dA, L, dB, X)
-        hL.copy_(L.mT, non_blocking=True)
-        hX.copy_(X.mT, non_blocking=True)
-
+    hA, hB = pinned_col_major(BATCH, N, N), pinned_col_major(BATCH, N, NRHS)
+    hA.copy_(A)
+    hB.copy_(B)
+    hL, hX = pinned_col_major(BATCH, N, N), pinned_col_major(BATCH, N, NRHS)
+    hinfo = torch.empty(BATCH, dtype=torch.int32, pin_memory=True)
+    del A, B, L, X
+    torch.cuda.empty_cache()
+    chunks = max(1, args.e2e_chunks)
+    pipe = PosvHostPipeline(N, NRHS, (BATCH + chunks - 1) // chunks, dev)
     for _ in range(2):
-        e2e_step()
+        pipe.run(hA, hB, hL, hX, hinfo)
     torch.cuda.synchronize()
     e2e_steps = max(2, min(args.steps, 10))
     barrier()
     e0.record(stream)
     for _ in range(e2e_steps):
-        e2e_step()
+        pipe.run(hA, hB, hL, hX, hinfo)
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / e2e_steps
@@ -378,7 +375,9 @@ def run_ours(args):
                      "kernel": "posv_thread_kernel"},
         "e2e": {"value": ws * BATCH / (e2e_ms * 1e-3), "unit": "matrices/s",
                 "h2d_bytes_per_step": hA.numel() * 8 + hB.numel() * 8,
-                "d2h_bytes_per_step": hL.numel() * 8 + hX.numel() * 8},
+                "d2h_bytes_per_step": hL.numel() * 8 + hX.numel() * 8 + BATCH * 4,
+                "ms_per_step": e2e_ms, "chunks": chunks,
+                "path": "blast_gb300.host.PosvHostPipeline (pinned host buffers, 3 streams)"},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
     }
@@ -397,6 +396,127 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def _timed(fn, steps, warm=2):
+    import torch
+
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def workload_gemm24(args):
+    """10,000 x (24x24x24) D = A*B + C, alpha = beta = 1, U[-1,1] (the gemm workload)."""
+    import numpy as np
+    import torch
+
+    import blast_gb300 as bg
+    from oracle import oracle as orc
+
+    batch, m = 10_000, 24
+    g = torch.Generator(device="cuda")
+    g.manual_seed(99)
+    A, B, C = (bg.col_major((batch,), m, m, "cuda") for _ in range(3))
+    for t in (A, B, C):
+        t.copy_(torch.rand(batch, m, m, generator=g, device="cuda", dtype=torch.float64) * 2 - 1)
+    D = bg.col_major((batch,), m, m, "cuda")
+    ms = _timed(lambda: bg.gemm(A, B, C, D), args.steps)
+    flops = 2.0 * m ** 3 * batch
+    # CPU: the oracle's restatement of BLAST's gemm, one instance per call, all host threads
+    hA, hB, hC = (t.cpu().numpy() for t in (A, B, C))
+    t0 = time.perf_counter()
+    reps = 0
+    while time.perf_counter() - t0 < 2.0:
+        orc.gemm_batch(1.0, hA, hB, 1.0, hC)
+        reps += 1
+    cpu = reps * batch / (time.perf_counter() - t0)
+    return {"workload": "gemm 10,000 x 24x24x24", "ms_per_step": ms, "matrices_per_s": batch / ms * 1e3,
+            "tflops": flops / ms / 1e9, "cpu_port_matrices_per_s": cpu, "cpu_threads": orc.max_threads()}
+
+
+def workload_lu_ragged(args):
+    """20,000 general matrices, n log-uniform in [4, 256], N(0,1), one RHS: getrf + getrs."""
+    import numpy as np
+    import torch
+
+    from blast_gb300.ragged import GesvPlan, Packed
+
+    rng = np.random.default_rng(2020)
+    count = 20_000
+    ns = np.floor(np.exp(rng.uniform(np.log(4), np.log(257), count))).astype(np.int64)
+    A = Packed(ns, ns, "cuda")
+    B = Packed(ns, np.ones_like(ns), "cuda")
+    g = torch.Generator(device="cuda")
+    g.manual_seed(2020)
+    A0 = torch.randn(A.buf.numel(), generator=g, device="cuda", dtype=torch.float64)
+    B0 = torch.randn(B.buf.numel(), generator=g, device="cuda", dtype=torch.float64)
+    plan = GesvPlan(A, B)
+
+    def step():
+        A.buf.copy_(A0)
+        B.buf.copy_(B0)
+        plan.run()
+
+    ms_copy = _timed(lambda: (A.buf.copy_(A0), B.buf.copy_(B0)), args.steps)
+    ms = _timed(step, args.steps) - ms_copy
+    flops = float(np.sum(2 * ns ** 3 / 3 - ns ** 2 / 2 + 5 * ns / 6 + 2 * ns ** 2 - ns))
+    return {"workload": "getrf+getrs ragged, 20,000 x n log-uniform [4,256]", "ms_per_step": ms,
+            "matrices_per_s": count / ms * 1e3, "tflops": flops / ms / 1e9,
+            "note": "time excludes re-copying the inputs (measured separately and subtracted)"}
+
+
+def workload_adjoint(args):
+    """8,192 SPD n ~ U{32..128} (A = G G^T + n I): forward solve and adjoint (factor kept)."""
+    import numpy as np
+    import torch
+
+    from blast_gb300 import _lib, desc
+    from blast_gb300.ragged import Packed, PosvPlan
+
+    rng = np.random.default_rng(55)
+    count = 8192
+    ns = rng.integers(32, 129, count)
+    A = Packed(ns, ns, "cuda")
+    g = torch.Generator(device="cuda")
+    g.manual_seed(55)
+    for n in np.unique(ns):
+        idx = np.nonzero(ns == n)[0]
+        G = torch.randn(len(idx), n, n, generator=g, device="cuda", dtype=torch.float64)
+        M = G @ G.mT + n * torch.eye(n, device="cuda", dtype=torch.float64)
+        for j, i in enumerate(idx):
+            A.view(int(i)).copy_(M[j])
+    ones = np.ones_like(ns)
+    B, X, T = Packed(ns, ones, "cuda"), Packed(ns, ones, "cuda"), Packed(ns, ones, "cuda")
+    B.buf.copy_(torch.randn(B.buf.numel(), generator=g, device="cuda", dtype=torch.float64))
+    T.buf.copy_(torch.randn(T.buf.numel(), generator=g, device="cuda", dtype=torch.float64))
+    L = Packed(ns, ns, "cuda")
+    fwd = PosvPlan(A, B, X, L)
+    G_, GB, GA = Packed(ns, ones, "cuda"), Packed(ns, ones, "cuda"), Packed(ns, ns, "cuda")
+    recs = np.zeros(count, dtype=desc.POSV_BWD_DTYPE)
+    order = np.argsort(-ns, kind="stable")
+    for slot, i in enumerate(order):
+        recs[slot] = (A.record(i), L.record(i), X.record(i), G_.record(i), GB.record(i), GA.record(i))
+    d = desc.upload(recs, "cuda")
+    info = torch.zeros(count, dtype=torch.int32, device="cuda")
+
+    def bwd():
+        torch.sub(X.buf, T.buf, out=G_.buf)  # dl/dx for l = |x - t|^2 / 2
+        _lib.call("blastgpu_dposv_bwd_batched", d.data_ptr(), count, int(ns.max()), 0, info.data_ptr(),
+                  torch.cuda.current_stream().cuda_stream)
+
+    ms_f = _timed(fwd.run, args.steps)
+    ms_b = _timed(bwd, args.steps)
+    return {"workload": "differentiable SPD solve, 8,192 x n ~ U{32..128}, 1 RHS",
+            "forward_ms": ms_f, "backward_ms": ms_b,
+            "forward_matrices_per_s": count / ms_f * 1e3, "backward_matrices_per_s": count / ms_b * 1e3}
 
 
 def run_mixed_only(args):
@@ -419,6 +539,11 @@ def main():
     ap.add_argument("--batch", type=int, default=BATCH, help="matrices per GPU (default 50,000)")
     ap.add_argument("--no-mixed", action="store_true",
                     help="skip the FP64-vs-mixed comparison on the ragged n in [64, 512] batch")
+    ap.add_argument("--workload", choices=["cholesky48", "gemm24", "lu_ragged", "adjoint"],
+                    default="cholesky48", help="cholesky48 (default) prints the contract line; the "
+                    "others print one JSON object for that workload")
+    ap.add_argument("--e2e-chunks", type=int, default=8,
+                    help="chunks of the host-buffer pipeline in the end-to-end leg")
     ap.add_argument("--only-mixed", action="store_true",
                     help="run only the FP64-vs-mixed comparison (with --mixed-count matrices)")
     ap.add_argument("--mixed-count", type=int, default=8192)
@@ -426,7 +551,13 @@ def main():
                     help="qr: the workload's Q diag(lambda) Q^T matrices; gram: G G^T/n + I, for "
                          "profilers under which torch.linalg cannot load")
     args = ap.parse_args()
-    if args.only_mixed:
+    if args.workload != "cholesky48":
+        import torch
+
+        torch.cuda.set_device(0)
+        fn = {"gemm24": workload_gemm24, "lu_ragged": workload_lu_ragged, "adjoint": workload_adjoint}
+        print(json.dumps(fn[args.workload](args)), flush=True)
+    elif args.only_mixed:
         run_mixed_only(args)
     elif args.impl == "reference":
         run_reference(args)

@@ -26,6 +26,8 @@
 // what the mixed path turns into matrices per second.
 #include <math_constants.h>
 
+#include <atomic>
+
 #include "common.cuh"
 
 namespace blastgpu {
@@ -34,7 +36,8 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kNB = 32;  // panel width = 4 columns per warp
-constexpr int kKC = 16;  // previous columns staged per pass of the panel update
+constexpr int kKC = 32;  // previous columns staged per pass of the panel update (= panel width,
+                         // so the staging buffer fits in the panel buffer's space)
 
 struct CtaItem {
     int n;
@@ -530,11 +533,21 @@ __global__ void __launch_bounds__(kThreads, 1) posv_bwd_kernel(Batch batch, int6
     }
 }
 
+// Raises a kernel's dynamic shared-memory limit once per process (before any stream capture
+// that replays the launch, the attribute is already set; setting it is not a stream operation).
+template <class K>
+cudaError_t ensure_smem(K kernel, size_t bytes) {
+    static std::atomic<size_t> done{0};
+    if (done.load(std::memory_order_acquire) >= bytes) return cudaSuccess;
+    cudaError_t const e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) done.store(bytes, std::memory_order_release);
+    return e;
+}
+
 template <int MAXR>
 int launch_bwd(DescBwd const& batch, int64_t count, int recompute, int32_t* info, cudaStream_t s) {
     size_t const smem = Smem<double, MAXR>::kBytes;
-    cudaError_t e = cudaFuncSetAttribute(posv_bwd_kernel<MAXR, DescBwd>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = ensure_smem(posv_bwd_kernel<MAXR, DescBwd>, smem);
     if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
     posv_bwd_kernel<MAXR, DescBwd><<<(unsigned)count, kThreads, smem, s>>>(batch, count, recompute, info);
     return check_launch();
@@ -545,10 +558,10 @@ int launch_cta(bool mixed, Batch const& batch, CtaArgs const& args, cudaStream_t
     size_t const smem = mixed ? Smem<float, MAXR>::kBytes : Smem<double, MAXR>::kBytes;
     cudaError_t e;
     if (mixed) {
-        e = cudaFuncSetAttribute(posv_cta_mixed_kernel<MAXR, Batch>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = ensure_smem(posv_cta_mixed_kernel<MAXR, Batch>, smem);
         if (e == cudaSuccess) posv_cta_mixed_kernel<MAXR, Batch><<<(unsigned)args.batch, kThreads, smem, s>>>(batch, args);
     } else {
-        e = cudaFuncSetAttribute(posv_cta_f64_kernel<MAXR, Batch>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = ensure_smem(posv_cta_f64_kernel<MAXR, Batch>, smem);
         if (e == cudaSuccess) posv_cta_f64_kernel<MAXR, Batch><<<(unsigned)args.batch, kThreads, smem, s>>>(batch, args);
     }
     if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }

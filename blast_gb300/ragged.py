@@ -95,16 +95,46 @@ class PosvPlan:
         self.iters = torch.zeros(self.count, dtype=torch.int32, device=device)
         self.berr = torch.zeros(self.count, dtype=torch.float64, device=device)
         self._keep = (A, B, X, L)
+        # Size bins (each launched with its own register tiling and shared-memory footprint, on
+        # its own stream so that the bins overlap): contiguous slices of the sorted order.
+        sorted_n = n[self.order]
+        self.bins = []
+        for lo, hi in ((257, 512), (129, 256), (65, 128), (0, 64)):
+            idx = np.nonzero((sorted_n >= lo) & (sorted_n <= hi))[0]
+            if len(idx):
+                self.bins.append((int(idx[0]), int(idx[-1]) + 1, int(sorted_n[idx[0]])))
+        self.streams = [torch.cuda.Stream(device) for _ in self.bins[1:]]
+
+    def _launch(self, b0, b1, max_n, s):
+        cnt = b1 - b0
+        dptr = self.d.data_ptr() + b0 * desc.POSV_DTYPE.itemsize
+        if self.mixed:
+            _lib.call("blastgpu_dposv_mixed_batched", dptr, cnt, max_n, self.workspace.data_ptr(),
+                      self.tol, self.max_iter, self.info.data_ptr() + 4 * b0,
+                      self.iters.data_ptr() + 4 * b0, self.berr.data_ptr() + 8 * b0, s)
+        else:
+            _lib.call("blastgpu_dposv_batched", dptr, cnt, max_n, self.info.data_ptr() + 4 * b0, s)
 
     def run(self, stream=None):
-        s = (stream or torch.cuda.current_stream()).cuda_stream
-        if self.mixed:
-            _lib.call("blastgpu_dposv_mixed_batched", self.d.data_ptr(), self.count, self.max_n,
-                      self.workspace.data_ptr(), self.tol, self.max_iter, self.info.data_ptr(),
-                      self.iters.data_ptr(), self.berr.data_ptr(), s)
-        else:
-            _lib.call("blastgpu_dposv_batched", self.d.data_ptr(), self.count, self.max_n,
-                      self.info.data_ptr(), s)
+        cur = stream or torch.cuda.current_stream()
+        if not self.bins:
+            return
+        # the largest bin on the caller's stream, the others forked and joined back
+        start = torch.cuda.Event()
+        start.record(cur)
+        for (b0, b1, mx), s in zip(self.bins[1:], self.streams):
+            s.wait_event(start)
+            self._launch(b0, b1, mx, s.cuda_stream)
+        b0, b1, mx = self.bins[0]
+        self._launch(b0, b1, mx, cur.cuda_stream)
+        for s in self.streams:
+            ev = torch.cuda.Event()
+            ev.record(s)
+            cur.wait_event(ev)
+
+    def capture(self):
+        """Records run() into a CUDA graph; returns the torch.cuda.CUDAGraph (call .replay())."""
+        return capture_graph(self.run)
 
     def results(self):
         """(info, iters, berr) as numpy arrays in the caller's instance order."""
@@ -114,6 +144,21 @@ class PosvPlan:
         iters = self.iters.cpu().numpy()[inv]
         berr = self.berr.cpu().numpy()[inv]
         return info, iters, berr
+
+
+def capture_graph(fn):
+    """Captures the stream work of fn() (launches through the C ABI, which neither allocate nor
+    synchronise) into a CUDA graph after one warm-up call."""
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        fn()
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        fn()
+    return g
 
 
 class GesvPlan:
@@ -137,6 +182,10 @@ class GesvPlan:
     def run(self, stream=None):
         s = (stream or torch.cuda.current_stream()).cuda_stream
         _lib.call("blastgpu_dgesv_batched", self.d.data_ptr(), self.info.data_ptr(), self.count, s)
+
+    def capture(self):
+        """Records run() into a CUDA graph; returns the torch.cuda.CUDAGraph (call .replay())."""
+        return capture_graph(self.run)
 
     def pivots(self):
         host = self.ipiv.buf.cpu().numpy()
