@@ -392,7 +392,10 @@ def run_ours(args):
     if ws == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline()
     if not args.no_mixed:
-        line["mixed_ir"] = mixed_ir_comparison(max(4, min(args.steps, 20)))
+        try:
+            line["mixed_ir"] = mixed_ir_comparison(max(4, min(args.steps, 20)))
+        except Exception as exc:  # the contract line must still be printed
+            line["mixed_ir"] = {"error": f"{type(exc).__name__}: {exc}"}
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()

@@ -535,11 +535,12 @@ __global__ void __launch_bounds__(kThreads, 1) posv_bwd_kernel(Batch batch, int6
 
 // Raises a kernel's dynamic shared-memory limit once per process (before any stream capture
 // that replays the launch, the attribute is already set; setting it is not a stream operation).
-template <class K>
-cudaError_t ensure_smem(K kernel, size_t bytes) {
+// The template parameter is the kernel itself, so every kernel has its own flag.
+template <auto Kernel>
+cudaError_t ensure_smem(size_t bytes) {
     static std::atomic<size_t> done{0};
     if (done.load(std::memory_order_acquire) >= bytes) return cudaSuccess;
-    cudaError_t const e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    cudaError_t const e = cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e == cudaSuccess) done.store(bytes, std::memory_order_release);
     return e;
 }
@@ -547,7 +548,7 @@ cudaError_t ensure_smem(K kernel, size_t bytes) {
 template <int MAXR>
 int launch_bwd(DescBwd const& batch, int64_t count, int recompute, int32_t* info, cudaStream_t s) {
     size_t const smem = Smem<double, MAXR>::kBytes;
-    cudaError_t e = ensure_smem(posv_bwd_kernel<MAXR, DescBwd>, smem);
+    cudaError_t e = ensure_smem<posv_bwd_kernel<MAXR, DescBwd>>(smem);
     if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
     posv_bwd_kernel<MAXR, DescBwd><<<(unsigned)count, kThreads, smem, s>>>(batch, count, recompute, info);
     return check_launch();
@@ -558,10 +559,10 @@ int launch_cta(bool mixed, Batch const& batch, CtaArgs const& args, cudaStream_t
     size_t const smem = mixed ? Smem<float, MAXR>::kBytes : Smem<double, MAXR>::kBytes;
     cudaError_t e;
     if (mixed) {
-        e = ensure_smem(posv_cta_mixed_kernel<MAXR, Batch>, smem);
+        e = ensure_smem<posv_cta_mixed_kernel<MAXR, Batch>>(smem);
         if (e == cudaSuccess) posv_cta_mixed_kernel<MAXR, Batch><<<(unsigned)args.batch, kThreads, smem, s>>>(batch, args);
     } else {
-        e = ensure_smem(posv_cta_f64_kernel<MAXR, Batch>, smem);
+        e = ensure_smem<posv_cta_f64_kernel<MAXR, Batch>>(smem);
         if (e == cudaSuccess) posv_cta_f64_kernel<MAXR, Batch><<<(unsigned)args.batch, kThreads, smem, s>>>(batch, args);
     }
     if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }

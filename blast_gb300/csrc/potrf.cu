@@ -25,27 +25,42 @@
 namespace blastgpu {
 namespace {
 
-// One KM x 4 register tile of the left-looking strip k (rows i .. i+KM-1).
-template <int KM>
-__device__ __forceinline__ void potrf_tile(int n, int k, int i, int nc, const double* A, int lda,
-                                           double* L, int ldl, double (&y)[4], bool diag, int& info) {
-    double acc[KM][4];
+// Addressing policies: BLAST's dense column-major storage and its panel storage with panel
+// height PS (element (i, j) at (i/PS)*spacing + i%PS + j*PS, panel/StaticPanelMatrix.hpp:178-184).
+struct ColAddr {
+    int64_t ld;
+    __device__ __forceinline__ int64_t operator()(int i, int j) const { return i + (int64_t)j * ld; }
+};
+
+template <int PS>
+struct PanelAddr {
+    int64_t spacing;
+    __device__ __forceinline__ int64_t operator()(int i, int j) const {
+        return (int64_t)(i / PS) * spacing + i % PS + (int64_t)j * PS;
+    }
+};
+
+// One KM x KN register tile of the left-looking strip k (rows i .. i+KM-1).
+template <int KM, int KN, class Addr>
+__device__ __forceinline__ void potrf_tile(int n, int k, int i, int nc, const double* A, Addr ia,
+                                           double* L, Addr il, double (&y)[KN], bool diag, int& info) {
+    double acc[KM][KN];
 #pragma unroll
-    for (int c = 0; c < 4; ++c)
+    for (int c = 0; c < KN; ++c)
 #pragma unroll
         for (int r = 0; r < KM; ++r)
-            acc[r][c] = (c < nc && i + r < n) ? A[(i + r) + (int64_t)(k + c) * lda] : 0.0;
+            acc[r][c] = (c < nc && i + r < n) ? A[ia(i + r, k + c)] : 0.0;
 
-    // acc -= L(i:i+KM, 0:k) * L(k:k+4, 0:k)^T, one fused rank-1 update per column l.
+    // acc -= L(i:i+KM, 0:k) * L(k:k+KN, 0:k)^T, one fused rank-1 update per column l
+    // (BLAST's ger(-1, ...) loop, dense/Potrf.hpp:40-41).
     for (int l = 0; l < k; ++l) {
-        double const* Ll = L + (int64_t)l * ldl;
-        double a[KM], b[4];
+        double a[KM], b[KN];
 #pragma unroll
-        for (int r = 0; r < KM; ++r) a[r] = (i + r < n) ? Ll[i + r] : 0.0;
+        for (int r = 0; r < KM; ++r) a[r] = (i + r < n) ? L[il(i + r, l)] : 0.0;
 #pragma unroll
-        for (int c = 0; c < 4; ++c) b[c] = (c < nc) ? Ll[k + c] : 0.0;
+        for (int c = 0; c < KN; ++c) b[c] = (c < nc) ? L[il(k + c, l)] : 0.0;
 #pragma unroll
-        for (int c = 0; c < 4; ++c)
+        for (int c = 0; c < KN; ++c)
 #pragma unroll
             for (int r = 0; r < KM; ++r) acc[r][c] = fma(-a[r], b[c], acc[r][c]);
     }
@@ -53,7 +68,7 @@ __device__ __forceinline__ void potrf_tile(int n, int k, int i, int nc, const do
     if (diag) {
         // In-register Cholesky of the strip (RegisterMatrix::potrf).
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
+        for (int c = 0; c < KN; ++c) {
             if (c < nc) {
 #pragma unroll
                 for (int j = 0; j < c; ++j) {
@@ -69,18 +84,18 @@ __device__ __forceinline__ void potrf_tile(int n, int k, int i, int nc, const do
             }
         }
 #pragma unroll
-        for (int c = 0; c < 4; ++c)
+        for (int c = 0; c < KN; ++c)
 #pragma unroll
             for (int r = 0; r < KM; ++r)
-                if (c < nc && r >= c && i + r < n) L[(i + r) + (int64_t)(k + c) * ldl] = acc[r][c];
+                if (c < nc && r >= c && i + r < n) L[il(i + r, k + c)] = acc[r][c];
     } else {
         // Right upper solve against the strip's diagonal block (RegisterMatrix::trsm).
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
+        for (int c = 0; c < KN; ++c) {
             if (c < nc) {
 #pragma unroll
                 for (int j = 0; j < c; ++j) {
-                    double const lcj = L[(k + c) + (int64_t)(k + j) * ldl];
+                    double const lcj = L[il(k + c, k + j)];
 #pragma unroll
                     for (int r = 0; r < KM; ++r) acc[r][c] = fma(-lcj, acc[r][j], acc[r][c]);
                 }
@@ -89,27 +104,30 @@ __device__ __forceinline__ void potrf_tile(int n, int k, int i, int nc, const do
             }
         }
 #pragma unroll
-        for (int c = 0; c < 4; ++c)
+        for (int c = 0; c < KN; ++c)
 #pragma unroll
             for (int r = 0; r < KM; ++r)
-                if (c < nc && i + r < n) L[(i + r) + (int64_t)(k + c) * ldl] = acc[r][c];
+                if (c < nc && i + r < n) L[il(i + r, k + c)] = acc[r][c];
     }
 }
 
-// Left-looking Cholesky of one n x n matrix; returns info (0 or first bad pivot + 1).
-__device__ int potrf_thread(int n, const double* A, int lda, double* L, int ldl) {
+// Left-looking Cholesky of one n x n matrix, strips of KN columns, row tiles of 3, 2 and 1 times
+// TS rows (dense: KN = TS = 4, dense/Potrf.hpp:87-105; panel: KN = min((RC-4)/3, SS), TS = SS,
+// panel/Potrf.hpp:84-105). Returns info (0 or first bad pivot + 1).
+template <int KN, int TS, class Addr>
+__device__ int potrf_thread(int n, const double* A, Addr ia, double* L, Addr il) {
     int info = 0;
-    for (int k = 0; k < n; k += 4) {
-        int const nc = min(4, n - k);
-        double y[4];
+    for (int k = 0; k < n; k += KN) {
+        int const nc = min(KN, n - k);
+        double y[KN];
         int i = k;
         while (i < n) {
             int const rem = n - i;
-            // BLAST's tile cover (dense/Potrf.hpp:97-104): 12 rows while more than 8 remain,
-            // then 8 while more than 4 remain, then 4.
-            if (rem > 8) { potrf_tile<12>(n, k, i, nc, A, lda, L, ldl, y, i == k, info); i += 12; }
-            else if (rem > 4) { potrf_tile<8>(n, k, i, nc, A, lda, L, ldl, y, i == k, info); i += 8; }
-            else { potrf_tile<4>(n, k, i, nc, A, lda, L, ldl, y, i == k, info); i += 4; }
+            // BLAST's tile cover: 3*TS rows while more than 2*TS remain, then 2*TS while more
+            // than TS remain, then TS.
+            if (rem > 2 * TS) { potrf_tile<3 * TS, KN>(n, k, i, nc, A, ia, L, il, y, i == k, info); i += 3 * TS; }
+            else if (rem > TS) { potrf_tile<2 * TS, KN>(n, k, i, nc, A, ia, L, il, y, i == k, info); i += 2 * TS; }
+            else { potrf_tile<TS, KN>(n, k, i, nc, A, ia, L, il, y, i == k, info); i += TS; }
         }
     }
     return info;
@@ -233,7 +251,7 @@ __global__ void __launch_bounds__(THREADS, MINB) posv_thread_kernel(PosvArgs p) 
     double* L = p.L + b * p.sl;
     int info = 0;
     if (p.mode != 2) {
-        info = potrf_thread(p.n, p.A + b * p.sa, p.lda, L, p.ldl);
+        info = potrf_thread<4, 4>(p.n, p.A + b * p.sa, ColAddr{p.lda}, L, ColAddr{p.ldl});
         if (p.info) p.info[b] = info;
     }
     if (p.mode != 0 && p.nrhs > 0) {
@@ -241,6 +259,26 @@ __global__ void __launch_bounds__(THREADS, MINB) posv_thread_kernel(PosvArgs p) 
         trsm_lower_thread(p.n, p.nrhs, L, p.ldl, p.B + b * p.sb, p.ldb, X, p.ldx);
         trsm_lower_trans_thread(p.n, p.nrhs, L, p.ldl, X, p.ldx);
     }
+}
+
+// Ragged potrf over descriptors whose matrices all have the layout `layout` (column-major, or
+// panel with panel height PS); one thread per matrix.
+template <int KN, int TS, class Addr>
+__global__ void __launch_bounds__(32, 12) potrf_desc_kernel(const blastgpu_potrf_desc* desc, int64_t count,
+                                                          int layout, int ps, int32_t* info) {
+    int64_t const b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= count) return;
+    blastgpu_potrf_desc const d = desc[b];
+    int const n = d.A.rows;
+    bool const ok = d.A.layout == layout && d.L.layout == layout && d.A.cols == n && d.L.rows == n &&
+                    d.L.cols == n && (layout == BLASTGPU_COL_MAJOR || (d.A.ps == ps && d.L.ps == ps));
+    if (!ok) {
+        if (info) info[b] = -1;
+        return;
+    }
+    Addr const ia{d.A.ld}, il{d.L.ld};
+    int const r = potrf_thread<KN, TS>(n, d.A.data, ia, d.L.data, il);
+    if (info) info[b] = r;
 }
 
 int launch_posv(PosvArgs const& p, cudaStream_t stream) {
@@ -285,6 +323,25 @@ int blastgpu_dpotrf_strided(int n, const double* A, int lda, int64_t stride_a, d
     if (batch < 0) return -9;
     PosvArgs p{n, 0, A, lda, stride_a, L, ldl, stride_l, nullptr, 1, 0, nullptr, 1, 0, info, batch, 0};
     return launch_posv(p, as_cuda(stream));
+}
+
+int blastgpu_dpotrf_batched(const blastgpu_potrf_desc* desc, int64_t batch, int layout, int ps,
+                            int32_t* info, blastgpu_stream_t stream) {
+    if (batch < 0) return -2;
+    if (layout != BLASTGPU_COL_MAJOR && layout != BLASTGPU_PANEL) return -3;
+    if (layout == BLASTGPU_PANEL && ps != 2 && ps != 4) return -4;
+    if (batch == 0) return BLASTGPU_SUCCESS;
+    if (!desc) return -1;
+    int64_t const blocks = (batch + 31) / 32;
+    if (blocks > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
+    cudaStream_t const s = as_cuda(stream);
+    if (layout == BLASTGPU_COL_MAJOR)
+        potrf_desc_kernel<4, 4, ColAddr><<<(unsigned)blocks, 32, 0, s>>>(desc, batch, layout, ps, info);
+    else if (ps == 4)  // AVX2 panels: SS = 4, 16 registers -> strips of min((16-4)/3, 4) = 4
+        potrf_desc_kernel<4, 4, PanelAddr<4>><<<(unsigned)blocks, 32, 0, s>>>(desc, batch, layout, ps, info);
+    else               // NEON panels: SS = 2, 32 registers -> strips of min((32-4)/3, 2) = 2
+        potrf_desc_kernel<2, 2, PanelAddr<2>><<<(unsigned)blocks, 32, 0, s>>>(desc, batch, layout, ps, info);
+    return check_launch();
 }
 
 int blastgpu_dposv_strided(int n, int nrhs, const double* A, int lda, int64_t stride_a, double* L,

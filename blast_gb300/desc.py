@@ -28,6 +28,12 @@ POSV_BWD_DTYPE = np.dtype([("A", MAT_DTYPE), ("L", MAT_DTYPE), ("X", MAT_DTYPE),
                            ("Xbar", MAT_DTYPE), ("Bbar", MAT_DTYPE), ("Abar", MAT_DTYPE)], align=True)
 assert POSV_BWD_DTYPE.itemsize == 192
 
+POTRF_DTYPE = np.dtype([("A", MAT_DTYPE), ("L", MAT_DTYPE)], align=True)
+assert POTRF_DTYPE.itemsize == 64
+
+COPY_DTYPE = np.dtype([("src", MAT_DTYPE), ("dst", MAT_DTYPE)], align=True)
+assert COPY_DTYPE.itemsize == 64
+
 EMPTY_MAT = (0, 0, 0, 1, 0, 0, 0)
 
 

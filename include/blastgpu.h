@@ -91,6 +91,20 @@ int blastgpu_selftest_recip(int which, const double* x, double* y, int n, blastg
 int blastgpu_probe_fp64_tflops(double* tflops, blastgpu_stream_t stream);
 
 /* ---------------------------------------------------------------------------------------------
+ * Layout conversion: dst = src element by element, for any pair of layouts (column-major,
+ * row-major, panel of height ps). Replaces BLAST's assign() between panel and dense matrices
+ * (expressions/PanelMatrix.hpp:63-240). Panel padding rows (beyond `rows`) are not written.
+ * status[b] (optional) = 0, or -1 if the instance's shapes differ.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct blastgpu_copy_desc {
+    blastgpu_mat src;
+    blastgpu_mat dst;
+} blastgpu_copy_desc; /* 64 bytes */
+
+int blastgpu_dcopy_batched(const blastgpu_copy_desc* desc, int64_t batch, int32_t* status,
+                           blastgpu_stream_t stream);
+
+/* ---------------------------------------------------------------------------------------------
  * gemm: D = alpha*A*B + beta*C
  * Replaces blast::gemm(alpha, A, B, beta, C, D)        (algorithm/Gemm.hpp:80-97),
  *          blast::gemm(A, B, C, D)                     (algorithm/Gemm.hpp:113-118, alpha=beta=1),
@@ -153,6 +167,19 @@ int blastgpu_dtrmm_strided(int side, int uplo, int unit, int m, int n, double al
 int blastgpu_dpotrf_strided(int n, const double* A, int lda, int64_t stride_a,
                             double* L, int ldl, int64_t stride_l, int32_t* info,
                             int64_t batch, blastgpu_stream_t stream);
+
+/* Ragged potrf over descriptors, including BLAST's panel storage. Every descriptor's A and L
+ * must have the given layout (BLASTGPU_COL_MAJOR, or BLASTGPU_PANEL with panel height ps = 4
+ * (AVX2 panels) or 2 (NEON panels)); instances that do not get info = -1. The panel variants run
+ * BLAST's panel algorithm (panel/Potrf.hpp:59-106): strips of KN = min((RC-4)/3, SS) columns
+ * (4 for ps = 4, 2 for ps = 2), row tiles of 3, 2 and 1 panels. */
+typedef struct blastgpu_potrf_desc {
+    blastgpu_mat A; /* n x n SPD input, lower triangle read */
+    blastgpu_mat L; /* n x n factor output (may equal A) */
+} blastgpu_potrf_desc; /* 64 bytes */
+
+int blastgpu_dpotrf_batched(const blastgpu_potrf_desc* desc, int64_t batch, int layout, int ps,
+                            int32_t* info, blastgpu_stream_t stream);
 
 /* potrf followed by the two triangular solves L*Y = B, L^T*X = Y (BLAST has no potrs; this is
  * potrf + trsm<Lower> + trsm<Upper> on trans(L), dense/Trsm.hpp:17-66), fused in one kernel.
