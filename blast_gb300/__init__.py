@@ -10,3 +10,19 @@ from .blast import (LEFT, LOWER, RIGHT, UPPER, col_major, gemm, getrf, getrs, po
 
 __all__ = ["gemm", "potrf", "posv", "potrs", "getrf", "getrs", "syrk_lower", "trsm", "trmm",
            "col_major", "LOWER", "UPPER", "LEFT", "RIGHT", "_lib"]
+
+
+def _apply_tuning():
+    """Loads the autotuner's cached per-bin choices for this GPU (blast_gb300/tuning/*.json)."""
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            from . import tune
+
+            tune.apply()
+    except (OSError, RuntimeError):
+        pass  # no library or no cache yet: the built-in defaults apply
+
+
+_apply_tuning()

@@ -59,9 +59,9 @@ SIGNATURES: dict[str, list] = {
     "blastgpu_dcopy_batched": [PTR, I64, PTR, PTR],
     "blastgpu_dgetrf_strided": [I32, I32, PTR, I32, I64, PTR, I64, PTR, I64, PTR],
     "blastgpu_dgetrs_strided": [I32, I32, PTR, I32, I64, PTR, I64, PTR, I32, I64, PTR, I64, PTR],
-    "blastgpu_dgetrf_batched": [PTR, PTR, I64, PTR],
+    "blastgpu_dgetrf_batched": [PTR, PTR, I64, I32, PTR],
     "blastgpu_dgetrs_batched": [PTR, PTR, I64, PTR],
-    "blastgpu_dgesv_batched": [PTR, PTR, I64, PTR],
+    "blastgpu_dgesv_batched": [PTR, PTR, I64, I32, PTR],
     "blastgpu_dposv_mixed_workspace_bytes": [I32],
     "blastgpu_dsyrk_lower_strided": [I32, I32, DBL, PTR, I32, I64, DBL, PTR, I32, I64, PTR, I32, I64, I64, PTR],
     "blastgpu_dtrsm_strided": [I32, I32, I32, I32, I32, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, I64, PTR],

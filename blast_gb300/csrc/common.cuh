@@ -31,6 +31,16 @@ int sm_count();
 // Kernel-selection parameters set by the autotuner (blastgpu_tune_set); `fallback` if unset.
 int tune_get(const char* key, int fallback);
 
+// Size bin of n for per-bin tuning keys: the smallest power of two >= n (at least 8).
+inline int size_bin(int n) {
+    int b = 8;
+    while (b < n && b < (1 << 20)) b <<= 1;
+    return b;
+}
+
+// tune_get(prefix + ".n" + size_bin(n)), falling back to tune_get(prefix), then to `fallback`.
+int tune_get_bin(const char* prefix, int n, int fallback);
+
 // ---------------------------------------------------------------------------------------------
 // Matrix views
 // ---------------------------------------------------------------------------------------------

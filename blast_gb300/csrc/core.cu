@@ -33,6 +33,12 @@ int tune_get(const char* key, int fallback) {
     return it == t.end() ? fallback : it->second;
 }
 
+int tune_get_bin(const char* prefix, int n, int fallback) {
+    std::string const base(prefix);
+    std::string const key = base + ".n" + std::to_string(size_bin(n));
+    return tune_get(key.c_str(), tune_get(base.c_str(), fallback));
+}
+
 int sm_count() {
     static std::mutex mu;
     static std::vector<int> cache;

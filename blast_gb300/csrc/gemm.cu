@@ -121,12 +121,19 @@ int launch_gemm(Batch const& batch, int64_t count, int max_m, int max_n, cudaStr
     int64_t const blocks64 = (count + kWarps - 1) / kWarps;
     if (blocks64 > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
     dim3 const grid((unsigned)blocks64), block(kWarps * 32);
-    // Warp-tile shape per size bin: the smallest tile that covers the instance without idle
-    // lanes where possible (24 x 24 is covered exactly by RM = 6, RN = 3).
-    if (max_m <= 8 && max_n <= 8) gemm_warp_kernel<2, 1><<<grid, block, 0, stream>>>(batch, count);
-    else if (max_m <= 16 && max_n <= 16) gemm_warp_kernel<4, 2><<<grid, block, 0, stream>>>(batch, count);
-    else if (max_m <= 24 && max_n <= 24) gemm_warp_kernel<6, 3><<<grid, block, 0, stream>>>(batch, count);
-    else gemm_warp_kernel<8, 4><<<grid, block, 0, stream>>>(batch, count);
+    // Warp-tile shape per size bin: by default the smallest tile that covers the instance
+    // without idle lanes where possible (24 x 24 is covered exactly by RM = 6, RN = 3); the
+    // autotuner may override it per bin ("gemm.shape.n<bin>": 0 = 8x8, 1 = 16x16, 2 = 24x24,
+    // 3 = 32x32 warp tiles).
+    int const mx = max_m > max_n ? max_m : max_n;
+    int const dflt = (max_m <= 8 && max_n <= 8) ? 0 : (max_m <= 16 && max_n <= 16) ? 1
+                   : (max_m <= 24 && max_n <= 24) ? 2 : 3;
+    switch (tune_get_bin("gemm.shape", mx, dflt)) {
+        case 0: gemm_warp_kernel<2, 1><<<grid, block, 0, stream>>>(batch, count); break;
+        case 1: gemm_warp_kernel<4, 2><<<grid, block, 0, stream>>>(batch, count); break;
+        case 2: gemm_warp_kernel<6, 3><<<grid, block, 0, stream>>>(batch, count); break;
+        default: gemm_warp_kernel<8, 4><<<grid, block, 0, stream>>>(batch, count); break;
+    }
     return check_launch();
 }
 

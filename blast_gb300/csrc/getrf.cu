@@ -170,6 +170,108 @@ __device__ int warp_getrf(GetrfItem it, int lane) {
     return 0;
 }
 
+// CTA-per-matrix getrf for larger n: the same steps as warp_getrf, with the panel factorised by
+// warp 0 and the swaps, U12 solve and trailing update spread over the whole CTA. In the trailing
+// update each thread owns rows, keeps the row's four A21 entries in registers and reads U12
+// (the same for all threads) from L1, so one fused chain per element costs one load and one
+// store; fewer matrices in flight keep the working set in L2.
+constexpr int kCtaThreads = 256;
+
+__device__ int cta_getrf(GetrfItem it, int* s_ret) {
+    constexpr int NB = 4;
+    int const M = it.m, N = it.n, lda = it.lda;
+    double* a = it.a;
+    int32_t* ipiv = it.ipiv;
+    int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    int k = 0;
+    for (; k + NB < M && k + NB < N; k += NB) {
+        if (warp == 0) {
+            int const r = warp_getf2(a, lda, k, k, M - k, NB, ipiv + k, lane);
+            __syncwarp();
+            if (lane < NB) ipiv[k + lane] += k;
+            if (lane == 0) *s_ret = r;
+        }
+        __syncthreads();
+        if (*s_ret) return k + *s_ret;
+        // laswp on the other columns, thread per column
+        for (int j = tid; j < N; j += kCtaThreads) {
+            if (j >= k && j < k + NB) continue;
+            double* p = a + (int64_t)j * lda;
+            for (int q = k; q < k + NB; ++q) {
+                int const pr = ipiv[q];
+                if (pr != q) {
+                    double const t = p[q];
+                    p[q] = p[pr];
+                    p[pr] = t;
+                }
+            }
+        }
+        __syncthreads();
+        // U12 := L11^{-1} A12, thread per column
+        for (int j = k + NB + tid; j < N; j += kCtaThreads) {
+            double* cj = a + (int64_t)j * lda;
+            double x[NB];
+#pragma unroll
+            for (int i = 0; i < NB; ++i) {
+                double acc = cj[k + i];
+#pragma unroll
+                for (int q = 0; q < i; ++q) acc = fma(-a[(k + i) + (int64_t)(k + q) * lda], x[q], acc);
+                x[i] = acc;
+                cj[k + i] = acc;
+            }
+        }
+        __syncthreads();
+        // A22 := A22 - A21 * U12, thread per row
+        for (int i = k + NB + tid; i < M; i += kCtaThreads) {
+            double l[NB];
+#pragma unroll
+            for (int q = 0; q < NB; ++q) l[q] = a[i + (int64_t)(k + q) * lda];
+            for (int j = k + NB; j < N; ++j) {
+                double const* u = a + k + (int64_t)j * lda;
+                double acc = 0.0;
+#pragma unroll
+                for (int q = 0; q < NB; ++q) acc = fma(l[q], u[q], acc);
+                double* c = a + i + (int64_t)j * lda;
+                *c = fma(1.0, *c, -acc);
+            }
+        }
+        __syncthreads();
+    }
+    if (k < M && k < N) {
+        if (warp == 0) {
+            int const r = warp_getf2(a, lda, k, k, M - k, N - k, ipiv + k, lane);
+            __syncwarp();
+            for (int i = k + lane; i < M && i < N; i += 32) ipiv[i] += k;
+            if (lane == 0) *s_ret = r;
+        }
+        __syncthreads();
+        if (*s_ret) return k + *s_ret;
+    }
+    for (int j = tid; j < k; j += kCtaThreads) {
+        double* p = a + (int64_t)j * lda;
+        for (int q = k; q < min(M, N); ++q) {
+            int const pr = ipiv[q];
+            if (pr != q) {
+                double const t = p[q];
+                p[q] = p[pr];
+                p[pr] = t;
+            }
+        }
+    }
+    __syncthreads();
+    return 0;
+}
+
+template <class Batch>
+__global__ void __launch_bounds__(kCtaThreads) getrf_cta_kernel(Batch batch, int64_t count, int32_t* info) {
+    __shared__ int s_ret;
+    int64_t const b = blockIdx.x;
+    if (b >= count) return;
+    GetrfItem const it = batch.get(b);
+    int const r = cta_getrf(it, &s_ret);
+    if (info && threadIdx.x == 0) info[b] = r;
+}
+
 template <class Batch>
 __global__ void __launch_bounds__(kWarps * 32) getrf_warp_kernel(Batch batch, int64_t count, int32_t* info) {
     int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -246,11 +348,19 @@ __global__ void __launch_bounds__(128) getrs_thread_kernel(Batch batch, int64_t 
     getrs_thread(it.n, it.nrhs, it.a, it.lda, it.ipiv, it.x, it.ldx);
 }
 
+// "getrf.cta.n<bin>" = 1 selects the CTA-per-matrix kernel for that size bin; by default it is
+// used above n = 64, the warp-per-matrix kernel below.
 template <class Batch>
-int launch_getrf(Batch const& batch, int64_t count, int32_t* info, cudaStream_t s) {
-    int64_t const blocks = (count + kWarps - 1) / kWarps;
-    if (blocks > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
-    getrf_warp_kernel<<<(unsigned)blocks, kWarps * 32, 0, s>>>(batch, count, info);
+int launch_getrf(Batch const& batch, int64_t count, int max_n, int32_t* info, cudaStream_t s) {
+    bool const cta = tune_get_bin("getrf.cta", max_n, max_n > 64 ? 1 : 0) != 0;
+    if (cta) {
+        if (count > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
+        getrf_cta_kernel<<<(unsigned)count, kCtaThreads, 0, s>>>(batch, count, info);
+    } else {
+        int64_t const blocks = (count + kWarps - 1) / kWarps;
+        if (blocks > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
+        getrf_warp_kernel<<<(unsigned)blocks, kWarps * 32, 0, s>>>(batch, count, info);
+    }
     return check_launch();
 }
 
@@ -286,15 +396,16 @@ int blastgpu_dgetrf_strided(int m, int n, double* A, int lda, int64_t stride_a, 
         return BLASTGPU_SUCCESS;
     }
     StridedGetrf g{m, n, lda, A, stride_a, ipiv, stride_ipiv};
-    return launch_getrf(g, batch, info, as_cuda(stream));
+    return launch_getrf(g, batch, m > n ? m : n, info, as_cuda(stream));
 }
 
 int blastgpu_dgetrf_batched(const blastgpu_getrf_desc* desc, int32_t* info, int64_t batch,
-                            blastgpu_stream_t stream) {
+                            int max_n, blastgpu_stream_t stream) {
     if (batch < 0) return -3;
     if (batch == 0) return BLASTGPU_SUCCESS;
     if (!desc) return -1;
-    return launch_getrf(DescGetrf{desc}, batch, info, as_cuda(stream));
+    if (max_n < 0) return -4;
+    return launch_getrf(DescGetrf{desc}, batch, max_n, info, as_cuda(stream));
 }
 
 int blastgpu_dgetrs_strided(int n, int nrhs, const double* LU, int lda, int64_t stride_a,
@@ -323,8 +434,8 @@ int blastgpu_dgetrs_batched(const blastgpu_getrf_desc* desc, const int32_t* info
 }
 
 int blastgpu_dgesv_batched(const blastgpu_getrf_desc* desc, int32_t* info, int64_t batch,
-                           blastgpu_stream_t stream) {
-    int st = blastgpu_dgetrf_batched(desc, info, batch, stream);
+                           int max_n, blastgpu_stream_t stream) {
+    int st = blastgpu_dgetrf_batched(desc, info, batch, max_n, stream);
     if (st != BLASTGPU_SUCCESS) return st;
     return blastgpu_dgetrs_batched(desc, info, batch, stream);
 }

@@ -20,8 +20,11 @@ __global__ void __launch_bounds__(128) copy_kernel(const blastgpu_copy_desc* des
     }
     MatView const s = view(d.src), t = view(d.dst);
     int const m = d.dst.rows, n = d.dst.cols;
-    int64_t const total = (int64_t)m * n;
     bool const row_major = d.dst.layout == BLASTGPU_ROW_MAJOR;
+    // a panel destination is walked slot by slot, padding rows of the last panel included
+    int64_t const total = d.dst.layout == BLASTGPU_PANEL
+                              ? (int64_t)((m + t.ps - 1) / t.ps) * t.ps * n
+                              : (int64_t)m * n;
     for (int64_t e = lane; e < total; e += 32) {
         int i, j;
         if (row_major) { i = (int)(e / n); j = (int)(e % n); }

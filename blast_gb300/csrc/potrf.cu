@@ -293,7 +293,7 @@ int launch_posv(PosvArgs const& p, cudaStream_t stream) {
     // Measured on GB300 at n = 48 (50,000 instances): 32 threads x 12 CTAs/SM is fastest
     // (4.29 ms vs 4.56 ms for 64 x 6 and 5.30 ms for 64 x 1); it lets the block scheduler even
     // out the per-SM load one warp at a time.
-    int const variant = tune_get("posv.variant", 3);
+    int const variant = tune_get_bin("posv.variant", p.n, 3);
     int const threads = variant == 2 ? 128 : variant == 3 ? 32 : 64;
     int64_t const blocks = (p.batch + threads - 1) / threads;
     if (blocks > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;

@@ -178,10 +178,33 @@ class GesvPlan:
         self.d = desc.upload(recs, device)
         self.info = torch.zeros(self.count, dtype=torch.int32, device=device)
         self._keep = (A, B)
+        # Two size bins for the factorisation (one CTA per matrix above n = 64, one warp per
+        # matrix below), on forked streams; the solves run as one launch afterwards.
+        sorted_n = n[self.order]
+        big = int(np.sum(sorted_n > 64))
+        self.bins = [(b0, b1, int(sorted_n[b0])) for b0, b1 in ((0, big), (big, self.count)) if b1 > b0]
+        self.side = torch.cuda.Stream(device)
+
+    def _getrf(self, b0, b1, max_n, s):
+        _lib.call("blastgpu_dgetrf_batched", self.d.data_ptr() + b0 * desc.GETRF_DTYPE.itemsize,
+                  self.info.data_ptr() + 4 * b0, b1 - b0, max_n, s)
 
     def run(self, stream=None):
-        s = (stream or torch.cuda.current_stream()).cuda_stream
-        _lib.call("blastgpu_dgesv_batched", self.d.data_ptr(), self.info.data_ptr(), self.count, s)
+        cur = stream or torch.cuda.current_stream()
+        if not self.bins:
+            return
+        if len(self.bins) == 2:
+            start = torch.cuda.Event()
+            start.record(cur)
+            self.side.wait_event(start)
+            self._getrf(*self.bins[1], self.side.cuda_stream)
+        self._getrf(*self.bins[0], cur.cuda_stream)
+        if len(self.bins) == 2:
+            done = torch.cuda.Event()
+            done.record(self.side)
+            cur.wait_event(done)
+        _lib.call("blastgpu_dgetrs_batched", self.d.data_ptr(), self.info.data_ptr(), self.count,
+                  cur.cuda_stream)
 
     def capture(self):
         """Records run() into a CUDA graph; returns the torch.cuda.CUDAGraph (call .replay())."""

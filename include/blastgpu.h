@@ -223,13 +223,15 @@ typedef struct blastgpu_getrf_desc {
     blastgpu_mat B;  /* n x nrhs right-hand sides, overwritten by X (getrs / gesv only) */
 } blastgpu_getrf_desc; /* 72 bytes */
 
+/* max_n bounds every instance's max(m, n) and selects the kernel: one warp per matrix for small
+ * sizes, one CTA per matrix above n = 64 (tunable per size bin). */
 int blastgpu_dgetrf_batched(const blastgpu_getrf_desc* desc, int32_t* info, int64_t batch,
-                            blastgpu_stream_t stream);
+                            int max_n, blastgpu_stream_t stream);
 int blastgpu_dgetrs_batched(const blastgpu_getrf_desc* desc, const int32_t* info, int64_t batch,
                             blastgpu_stream_t stream);
 /* getrf followed by getrs on every instance (two launches on `stream`). */
 int blastgpu_dgesv_batched(const blastgpu_getrf_desc* desc, int32_t* info, int64_t batch,
-                           blastgpu_stream_t stream);
+                           int max_n, blastgpu_stream_t stream);
 
 /* ---------------------------------------------------------------------------------------------
  * Ragged Cholesky solves, n <= 512, one CTA per matrix, one launch for the whole batch.

@@ -20,8 +20,9 @@ def _oracle_lu(orc, A):
 
 
 @pytest.mark.parametrize("m,n", [(1, 1), (2, 2), (3, 3), (4, 4), (5, 5), (8, 8), (9, 9), (12, 12),
-                                 (17, 17), (33, 33), (48, 48), (64, 64), (100, 100), (256, 256),
-                                 (7, 3), (3, 7), (40, 21), (21, 40)])
+                                 (17, 17), (33, 33), (48, 48), (64, 64), (65, 65), (100, 100),
+                                 (256, 256), (7, 3), (3, 7), (40, 21), (21, 40), (90, 70), (70, 90),
+                                 (300, 129)])
 def test_getrf_uniform_bitexact(gpu, oracle_lib, m, n):
     import torch
 
@@ -120,7 +121,7 @@ def test_gesv_ragged_log_uniform(gpu, oracle_lib):
         pivs.append(p)
     d = desc.upload(recs, "cuda")
     info = torch.full((count,), -7, dtype=torch.int32, device="cuda")
-    _lib.call("blastgpu_dgesv_batched", d.data_ptr(), info.data_ptr(), count,
+    _lib.call("blastgpu_dgesv_batched", d.data_ptr(), info.data_ptr(), count, int(ns.max()),
               torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
     assert not info.cpu().numpy().any()
