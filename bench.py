@@ -211,7 +211,7 @@ def mixed_ir_comparison(steps: int, count: int = 8192, gen: str = "qr"):
 
 
 def load_traffic():
-    p = ROOT / "profiles" / "posv_n48_traffic.json"
+    p = ROOT / "profiles" / "posv_thread_n48_traffic.json"
     if p.exists():
         try:
             return json.loads(p.read_text())

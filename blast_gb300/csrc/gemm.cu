@@ -13,6 +13,8 @@
 // scaling, fma(beta, c, .)), so the results are bit-identical to the oracle restatement.
 // GB300's binary64 pipe (~1.2 TFLOP/s measured) bounds this kernel; the staging and shared-memory
 // traffic are far below their own limits.
+#include <cstdio>
+
 #include "common.cuh"
 
 namespace blastgpu {
@@ -123,12 +125,14 @@ int launch_gemm(Batch const& batch, int64_t count, int max_m, int max_n, cudaStr
     dim3 const grid((unsigned)blocks64), block(kWarps * 32);
     // Warp-tile shape per size bin: by default the smallest tile that covers the instance
     // without idle lanes where possible (24 x 24 is covered exactly by RM = 6, RN = 3); the
-    // autotuner may override it per bin ("gemm.shape.n<bin>": 0 = 8x8, 1 = 16x16, 2 = 24x24,
-    // 3 = 32x32 warp tiles).
+    // autotuner may override it per bin (0 = 8x8, 1 = 16x16, 2 = 24x24, 3 = 32x32 warp tiles).
     int const mx = max_m > max_n ? max_m : max_n;
     int const dflt = (max_m <= 8 && max_n <= 8) ? 0 : (max_m <= 16 && max_n <= 16) ? 1
                    : (max_m <= 24 && max_n <= 24) ? 2 : 3;
-    switch (tune_get_bin("gemm.shape", mx, dflt)) {
+    // gemm tiles change every 8 rows/columns, so its bins are multiples of 8 ("gemm.shape.m24").
+    char key[32];
+    snprintf(key, sizeof(key), "gemm.shape.m%d", ((mx + 7) / 8) * 8);
+    switch (tune_get(key, dflt)) {
         case 0: gemm_warp_kernel<2, 1><<<grid, block, 0, stream>>>(batch, count); break;
         case 1: gemm_warp_kernel<4, 2><<<grid, block, 0, stream>>>(batch, count); break;
         case 2: gemm_warp_kernel<6, 3><<<grid, block, 0, stream>>>(batch, count); break;

@@ -5,11 +5,12 @@ Tunable choices (read by the library through blastgpu_tune_set / tune_get_bin):
 * ``posv.variant.n<bin>`` — thread-per-matrix Cholesky solve: CTA size and the register budget
   the kernel is compiled for (0: 64 threads, 213 registers; 1: 64 x 168; 2: 128 x 168;
   3: 32 x 168).
-* ``gemm.shape.n<bin>`` — warp tile of the batched gemm (0: 8x8, 1: 16x16, 2: 24x24, 3: 32x32).
+* ``gemm.shape.m<8k>`` — warp tile of the batched gemm (0: 8x8, 1: 16x16, 2: 24x24, 3: 32x32),
+  per largest dimension rounded up to a multiple of 8.
 
 Results are cached as JSON keyed by GPU name (``blast_gb300/tuning/<gpu>.json``); ``apply()``
 loads the cache for the current GPU into the library, and ``import blast_gb300`` calls it.
-Bins are powers of two (the smallest power of two >= n, at least 8).
+Cholesky bins are powers of two (the smallest power of two >= n, at least 8).
 """
 from __future__ import annotations
 
@@ -94,7 +95,7 @@ def tune_posv(ns=(8, 16, 24, 32, 48, 64), nrhs=8, batch=50_000, variants=(0, 1, 
     return out
 
 
-def tune_gemm(sizes=(8, 16, 24, 32, 48, 64), batch=10_000, shapes=(0, 1, 2, 3)) -> dict:
+def tune_gemm(sizes=(8, 16, 24, 32, 40, 48, 56, 64), batch=10_000, shapes=(0, 1, 2, 3)) -> dict:
     from .blast import col_major, gemm
 
     out = {}
@@ -102,7 +103,7 @@ def tune_gemm(sizes=(8, 16, 24, 32, 48, 64), batch=10_000, shapes=(0, 1, 2, 3)) 
         A, B, C, D = (col_major((batch,), m, m, "cuda") for _ in range(4))
         for t in (A, B, C):
             t.copy_(torch.rand(batch, m, m, device="cuda", dtype=torch.float64))
-        key = f"gemm.shape.n{size_bin(m)}"
+        key = f"gemm.shape.m{(m + 7) // 8 * 8}"
         times = {}
         for sh in shapes:
             _lib.tune_set(key, sh)
