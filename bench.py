@@ -453,7 +453,7 @@ def workload_lu_ragged(args):
     from blast_gb300.ragged import GesvPlan, Packed
 
     rng = np.random.default_rng(2020)
-    count = 20_000
+    count = args.count or 20_000
     ns = np.floor(np.exp(rng.uniform(np.log(4), np.log(257), count))).astype(np.int64)
     A = Packed(ns, ns, "cuda")
     B = Packed(ns, np.ones_like(ns), "cuda")
@@ -545,6 +545,8 @@ def main():
     ap.add_argument("--workload", choices=["cholesky48", "gemm24", "lu_ragged", "adjoint"],
                     default="cholesky48", help="cholesky48 (default) prints the contract line; the "
                     "others print one JSON object for that workload")
+    ap.add_argument("--count", type=int, default=0,
+                    help="instances for --workload lu_ragged (default 20,000; smaller for profiling)")
     ap.add_argument("--e2e-chunks", type=int, default=8,
                     help="chunks of the host-buffer pipeline in the end-to-end leg")
     ap.add_argument("--only-mixed", action="store_true",

@@ -59,6 +59,18 @@ struct DescPosv {
     }
 };
 
+// Asynchronous global -> shared copies (cp.async, completed by cp_async_wait_all + a barrier):
+// every thread issues all of its copies back to back instead of waiting for each load.
+__device__ __forceinline__ void cp_async(float* dst, const float* src) {
+    unsigned const d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async(double* dst, const double* src) {
+    unsigned const d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 template <typename T>
 __device__ __forceinline__ T rsqrt_t(T s);
 template <>
@@ -140,8 +152,9 @@ __device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf,
             __syncthreads();
             for (int q = 0; q < kc; ++q) {
                 T const* src = F + k0 + (int64_t)(kk + q) * ldf;
-                for (int r = tid; r < m; r += kThreads) buf[q * NMAX + r] = src[r];
+                for (int r = tid; r < m; r += kThreads) cp_async(buf + q * NMAX + r, src + r);
             }
+            cp_async_wait_all();
             __syncthreads();
             for (int q = 0; q < kc; ++q) {
                 T const* col = buf + q * NMAX;
@@ -219,8 +232,10 @@ template <typename T>
 __device__ __forceinline__ void stage_block(const T* F, int ldf, int j0, int nb, T* blk) {
     for (int idx = threadIdx.x; idx < 32 * 32; idx += kThreads) {
         int const r = idx & 31, c = idx >> 5;
-        blk[c * 33 + r] = (r < nb && c < nb) ? F[(j0 + r) + (int64_t)(j0 + c) * ldf] : (T)(r == c ? 1 : 0);
+        if (r < nb && c < nb) cp_async(blk + c * 33 + r, F + (j0 + r) + (int64_t)(j0 + c) * ldf);
+        else blk[c * 33 + r] = (T)(r == c ? 1 : 0);
     }
+    cp_async_wait_all();
 }
 
 // In-place solve with the factor: v := F^{-T} F^{-1} v (v in shared memory, precision T).
@@ -228,6 +243,7 @@ __device__ __forceinline__ void stage_block(const T* F, int ldf, int j0, int nb,
 // columns for the backward pass), fully unrolled; the other rows are updated by all threads.
 template <typename T, int MAXR>
 __device__ void cta_potrs(int n, const T* F, int ldf, T* v, T* blk) {
+    __shared__ T red[kWarps * 32];
     int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // forward: F * y = v
     for (int j0 = 0; j0 < n; j0 += 32) {
@@ -262,14 +278,33 @@ __device__ void cta_potrs(int n, const T* F, int ldf, T* v, T* blk) {
     int const last = ((n - 1) / 32) * 32;
     for (int j0 = last; j0 >= 0; j0 -= 32) {
         int const nb = min(32, n - j0);
-        // rows of this block take the contributions of the rows below: v_i -= sum_r F(r,i) v_r
+        // rows of this block take the contributions of the rows below: v_i -= sum_r F(r,i) v_r.
+        // Every thread takes rows r = j0+nb+tid, +256, ... and accumulates all 32 columns (loads
+        // coalesced across threads for each column, all independent); the 8 warps' partial sums
+        // are then reduced through shared memory (red: 8 x 32 values).
         if (j0 + nb < n) {
-            for (int i = warp; i < nb; i += kWarps) {
-                T acc = (T)0;
-                for (int r = j0 + nb + lane; r < n; r += 32) acc = fma(F[r + (int64_t)(j0 + i) * ldf], v[r], acc);
+            T part[32];
 #pragma unroll
-                for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-                if (lane == 0) v[j0 + i] -= acc;
+            for (int i = 0; i < 32; ++i) part[i] = (T)0;
+            for (int r = j0 + nb + tid; r < n; r += kThreads) {
+                T const vr = v[r];
+                T const* row = F + r + (int64_t)j0 * ldf;
+#pragma unroll
+                for (int i = 0; i < 32; ++i)
+                    if (i < nb) part[i] = fma(row[(int64_t)i * ldf], vr, part[i]);
+            }
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+                T x = part[i];
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+                if (lane == i) red[warp * 32 + i] = x;
+            }
+            __syncthreads();
+            if (tid < nb) {
+                T acc = (T)0;
+                for (int w = 0; w < kWarps; ++w) acc += red[w * 32 + tid];
+                v[j0 + tid] -= acc;
             }
         }
         stage_block<T>(F, ldf, j0, nb, blk);
@@ -316,15 +351,35 @@ __device__ void cta_symv_lower(int n, const double* A, int lda, const double* x,
     int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int p = tid; p < (n + 1) / 2; p += kThreads) {
         int const q = n - 1 - p;
-        double a0 = 0.0, a1 = 0.0;
-        for (int j = 0; j <= p; ++j) {
-            double const xj = x[j];
-            a0 = fma(A[p + (int64_t)j * lda], xj, a0);
-            a1 = fma(A[q + (int64_t)j * lda], xj, a1);
+        double a0[4] = {0.0, 0.0, 0.0, 0.0}, a1[4] = {0.0, 0.0, 0.0, 0.0};
+        int j = 0;
+        for (; j + 3 <= p; j += 4) {
+            double ap[4], aq[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                ap[u] = A[p + (int64_t)(j + u) * lda];
+                aq[u] = A[q + (int64_t)(j + u) * lda];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                a0[u] = fma(ap[u], x[j + u], a0[u]);
+                a1[u] = fma(aq[u], x[j + u], a1[u]);
+            }
         }
-        for (int j = p + 1; j <= q; ++j) a1 = fma(A[q + (int64_t)j * lda], x[j], a1);
-        y[p] = a0;
-        if (q != p) y[q] = a1;
+        for (; j <= p; ++j) {
+            a0[0] = fma(A[p + (int64_t)j * lda], x[j], a0[0]);
+            a1[0] = fma(A[q + (int64_t)j * lda], x[j], a1[0]);
+        }
+        for (; j + 3 <= q; j += 4) {
+            double aq[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) aq[u] = A[q + (int64_t)(j + u) * lda];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) a1[u] = fma(aq[u], x[j + u], a1[u]);
+        }
+        for (; j <= q; ++j) a1[0] = fma(A[q + (int64_t)j * lda], x[j], a1[0]);
+        y[p] = (a0[0] + a0[1]) + (a0[2] + a0[3]);
+        if (q != p) y[q] = (a1[0] + a1[1]) + (a1[2] + a1[3]);
     }
     __syncthreads();
     for (int i = warp; i < n; i += kWarps) {
@@ -397,14 +452,35 @@ __global__ void __launch_bounds__(kThreads, 2) posv_cta_mixed_kernel(Batch batch
     {
         for (int p = tid; p < (n + 1) / 2; p += kThreads) {
             int const q = n - 1 - p;
-            double s0 = 0.0, s1 = 0.0;
-            for (int j = 0; j <= p; ++j) {
-                s0 += fabs(it.A[p + (int64_t)j * it.lda]);
-                s1 += fabs(it.A[q + (int64_t)j * it.lda]);
+            double s0[4] = {0.0, 0.0, 0.0, 0.0}, s1[4] = {0.0, 0.0, 0.0, 0.0};
+            int j = 0;
+            for (; j + 3 <= p; j += 4) {
+                double ap[4], aq[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    ap[u] = it.A[p + (int64_t)(j + u) * it.lda];
+                    aq[u] = it.A[q + (int64_t)(j + u) * it.lda];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    s0[u] += fabs(ap[u]);
+                    s1[u] += fabs(aq[u]);
+                }
             }
-            for (int j = p + 1; j <= q; ++j) s1 += fabs(it.A[q + (int64_t)j * it.lda]);
-            r[p] = s0;
-            if (q != p) r[q] = s1;
+            for (; j <= p; ++j) {
+                s0[0] += fabs(it.A[p + (int64_t)j * it.lda]);
+                s1[0] += fabs(it.A[q + (int64_t)j * it.lda]);
+            }
+            for (; j + 3 <= q; j += 4) {
+                double aq[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) aq[u] = it.A[q + (int64_t)(j + u) * it.lda];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) s1[u] += fabs(aq[u]);
+            }
+            for (; j <= q; ++j) s1[0] += fabs(it.A[q + (int64_t)j * it.lda]);
+            r[p] = (s0[0] + s0[1]) + (s0[2] + s0[3]);
+            if (q != p) r[q] = (s1[0] + s1[1]) + (s1[2] + s1[3]);
         }
         __syncthreads();
         int const lane = tid & 31, warp = tid >> 5;
