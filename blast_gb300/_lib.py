@@ -6,10 +6,12 @@ raises, so a test or benchmark can never silently run something other than the C
 from __future__ import annotations
 
 import ctypes as C
+import os
 import threading
 from pathlib import Path
 
-LIB_PATH = Path(__file__).resolve().parent / "lib" / "libblastgpu.so"
+# The in-tree build; BLASTGPU_LIBRARY may name another build of the same ABI.
+LIB_PATH = Path(os.environ.get("BLASTGPU_LIBRARY") or Path(__file__).resolve().parent / "lib" / "libblastgpu.so")
 
 _lib = None
 _lock = threading.Lock()

@@ -177,7 +177,9 @@ __device__ int warp_getrf(GetrfItem it, int lane) {
 // store; fewer matrices in flight keep the working set in L2.
 constexpr int kCtaThreads = 256;
 
-__device__ int cta_getrf(GetrfItem it, int* s_ret) {
+constexpr int kPanelRows = 512;  // panels up to this height are factored in shared memory
+
+__device__ int cta_getrf(GetrfItem it, int* s_ret, double* sp) {
     constexpr int NB = 4;
     int const M = it.m, N = it.n, lda = it.lda;
     double* a = it.a;
@@ -185,7 +187,27 @@ __device__ int cta_getrf(GetrfItem it, int* s_ret) {
     int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     int k = 0;
     for (; k + NB < M && k + NB < N; k += NB) {
-        if (warp == 0) {
+        int const mk = M - k;
+        if (mk <= kPanelRows) {
+            // The (M-k) x 4 panel goes to shared memory, is factored there by warp 0 (same
+            // operations, shared-memory latency instead of global), and is written back.
+            for (int idx = tid; idx < NB * mk; idx += kCtaThreads) {
+                int const c = idx / mk, r = idx - c * mk;
+                sp[c * kPanelRows + r] = a[(k + r) + (int64_t)(k + c) * lda];
+            }
+            __syncthreads();
+            if (warp == 0) {
+                int const r = warp_getf2(sp, kPanelRows, 0, 0, mk, NB, ipiv + k, lane);
+                __syncwarp();
+                if (lane < NB) ipiv[k + lane] += k;
+                if (lane == 0) *s_ret = r;
+            }
+            __syncthreads();
+            for (int idx = tid; idx < NB * mk; idx += kCtaThreads) {
+                int const c = idx / mk, r = idx - c * mk;
+                a[(k + r) + (int64_t)(k + c) * lda] = sp[c * kPanelRows + r];
+            }
+        } else if (warp == 0) {
             int const r = warp_getf2(a, lda, k, k, M - k, NB, ipiv + k, lane);
             __syncwarp();
             if (lane < NB) ipiv[k + lane] += k;
@@ -265,10 +287,11 @@ __device__ int cta_getrf(GetrfItem it, int* s_ret) {
 template <class Batch>
 __global__ void __launch_bounds__(kCtaThreads) getrf_cta_kernel(Batch batch, int64_t count, int32_t* info) {
     __shared__ int s_ret;
+    __shared__ double s_panel[4 * kPanelRows];
     int64_t const b = blockIdx.x;
     if (b >= count) return;
     GetrfItem const it = batch.get(b);
-    int const r = cta_getrf(it, &s_ret);
+    int const r = cta_getrf(it, &s_ret, s_panel);
     if (info && threadIdx.x == 0) info[b] = r;
 }
 
