@@ -40,10 +40,13 @@ struct PanelAddr {
     }
 };
 
-// One KM x KN register tile of the left-looking strip k (rows i .. i+KM-1).
-template <int KM, int KN, class Addr>
+// One KM x KN register tile of the left-looking strip k (rows i .. i+KM-1). DIAG: the strip's
+// first tile, which holds the diagonal block; its strictly upper entries (r < c) are never stored,
+// so their fused multiply-adds are left out at compile time.
+template <int KM, int KN, bool DIAG, class Addr>
 __device__ __forceinline__ void potrf_tile(int n, int k, int i, int nc, const double* A, Addr ia,
-                                           double* L, Addr il, double (&y)[KN], bool diag, int& info) {
+                                           double* L, Addr il, double (&y)[KN], int& info) {
+    constexpr bool diag = DIAG;
     double acc[KM][KN];
 #pragma unroll
     for (int c = 0; c < KN; ++c)
@@ -62,7 +65,8 @@ __device__ __forceinline__ void potrf_tile(int n, int k, int i, int nc, const do
 #pragma unroll
         for (int c = 0; c < KN; ++c)
 #pragma unroll
-            for (int r = 0; r < KM; ++r) acc[r][c] = fma(-a[r], b[c], acc[r][c]);
+            for (int r = 0; r < KM; ++r)
+                if (!DIAG || r >= c) acc[r][c] = fma(-a[r], b[c], acc[r][c]);
     }
 
     if (diag) {
@@ -74,13 +78,15 @@ __device__ __forceinline__ void potrf_tile(int n, int k, int i, int nc, const do
                 for (int j = 0; j < c; ++j) {
                     double const lcj = acc[c][j];
 #pragma unroll
-                    for (int r = 0; r < KM; ++r) acc[r][c] = fma(-lcj, acc[r][j], acc[r][c]);
+                    for (int r = 0; r < KM; ++r)
+                        if (r >= c) acc[r][c] = fma(-lcj, acc[r][j], acc[r][c]);
                 }
                 double const s = acc[c][c];
                 if (!(s > 0.0) && info == 0) info = k + c + 1;
                 y[c] = rsqrt_nr(s);
 #pragma unroll
-                for (int r = 0; r < KM; ++r) acc[r][c] *= y[c];
+                for (int r = 0; r < KM; ++r)
+                    if (r >= c) acc[r][c] *= y[c];
             }
         }
 #pragma unroll
@@ -125,9 +131,20 @@ __device__ int potrf_thread(int n, const double* A, Addr ia, double* L, Addr il)
             int const rem = n - i;
             // BLAST's tile cover: 3*TS rows while more than 2*TS remain, then 2*TS while more
             // than TS remain, then TS.
-            if (rem > 2 * TS) { potrf_tile<3 * TS, KN>(n, k, i, nc, A, ia, L, il, y, i == k, info); i += 3 * TS; }
-            else if (rem > TS) { potrf_tile<2 * TS, KN>(n, k, i, nc, A, ia, L, il, y, i == k, info); i += 2 * TS; }
-            else { potrf_tile<TS, KN>(n, k, i, nc, A, ia, L, il, y, i == k, info); i += TS; }
+            bool const first = i == k;
+            if (rem > 2 * TS) {
+                if (first) potrf_tile<3 * TS, KN, true>(n, k, i, nc, A, ia, L, il, y, info);
+                else potrf_tile<3 * TS, KN, false>(n, k, i, nc, A, ia, L, il, y, info);
+                i += 3 * TS;
+            } else if (rem > TS) {
+                if (first) potrf_tile<2 * TS, KN, true>(n, k, i, nc, A, ia, L, il, y, info);
+                else potrf_tile<2 * TS, KN, false>(n, k, i, nc, A, ia, L, il, y, info);
+                i += 2 * TS;
+            } else {
+                if (first) potrf_tile<TS, KN, true>(n, k, i, nc, A, ia, L, il, y, info);
+                else potrf_tile<TS, KN, false>(n, k, i, nc, A, ia, L, il, y, info);
+                i += TS;
+            }
         }
     }
     return info;
