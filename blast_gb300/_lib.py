@@ -40,6 +40,8 @@ class blastgpu_gemm_desc(C.Structure):
 
 I32, I64, DBL, PTR = C.c_int, C.c_int64, C.c_double, C.c_void_p
 
+NOALLOC_SCRATCH_BYTES = 32 << 20  # BLASTGPU_NOALLOC_SCRATCH_BYTES in include/blastgpu.h
+
 # name -> argtypes (restype is int unless listed in _RESTYPES)
 SIGNATURES: dict[str, list] = {
     "blastgpu_version": [],
@@ -71,6 +73,7 @@ SIGNATURES: dict[str, list] = {
     "blastgpu_dposv_batched": [PTR, I64, I32, PTR, PTR],
     "blastgpu_dposv_mixed_batched": [PTR, I64, I32, PTR, DBL, I32, PTR, PTR, PTR, PTR],
     "blastgpu_dposv_bwd_batched": [PTR, I64, I32, I32, PTR, PTR],
+    "blastgpu_dposv_mixed_batched_noalloc": [PTR, I64, I32, C.c_size_t, DBL, I32, PTR, PTR, PTR, PTR],
 }
 _RESTYPES = {"blastgpu_status_string": C.c_char_p, "blastgpu_launch_count": C.c_int64,
              "blastgpu_dposv_mixed_workspace_bytes": C.c_size_t}

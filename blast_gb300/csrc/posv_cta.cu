@@ -27,6 +27,7 @@
 #include <math_constants.h>
 
 #include <atomic>
+#include <mutex>
 
 #include "common.cuh"
 
@@ -656,12 +657,56 @@ int dispatch_cta(bool mixed, int max_n, Batch const& batch, CtaArgs const& args,
     return BLASTGPU_ERR_TOO_LARGE;
 }
 
+// Scratch for blastgpu_dposv_mixed_batched_noalloc: a fixed array in the module's device memory,
+// reserved on every GPU that loads the library until the process exits. It holds the binary32
+// factors of one call; every call reuses it, so calls whose kernels overlap on the GPU race.
+constexpr size_t kNoAllocScratchBytes = BLASTGPU_NOALLOC_SCRATCH_BYTES;  // 32 MiB
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Device address of g_noalloc_scratch on the current device, looked up once per device (the
+// host-side symbol is only a stand-in and must not be passed to a kernel).
+cudaError_t noalloc_scratch(void** out) {
+    static std::mutex mu;
+    static void* addr[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        addr[dev] = p;
+    }
+    *out = addr[dev];
+    return cudaSuccess;
+}
+
 }  // namespace
 }  // namespace blastgpu
 
 using namespace blastgpu;
 
 extern "C" {
+
+int blastgpu_dposv_mixed_batched_noalloc(const blastgpu_posv_desc* desc, int64_t batch, int max_n,
+                                         size_t scratch_bytes, double tol, int max_iter, int32_t* info,
+                                         int32_t* iters, double* berr, blastgpu_stream_t stream) {
+    if (batch < 0) return -2;
+    if (batch == 0) return BLASTGPU_SUCCESS;
+    if (!desc) return -1;
+    if (max_n < 0) return -3;
+    if (max_n > 512) return BLASTGPU_ERR_TOO_LARGE;
+    if (scratch_bytes > kNoAllocScratchBytes) return BLASTGPU_ERR_TOO_LARGE;
+    if (!(tol >= 0.0)) return -5;
+    if (max_iter < 0) return -6;
+    void* scratch = nullptr;
+    cudaError_t const e = noalloc_scratch(&scratch);
+    if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
+    CtaArgs a{batch, info, iters, berr, tol, max_iter};
+    return dispatch_cta(true, max_n, DescPosv{desc, static_cast<char*>(scratch)}, a, as_cuda(stream));
+}
 
 size_t blastgpu_dposv_mixed_workspace_bytes(int n) {
     if (n <= 0) return 0;

@@ -262,6 +262,28 @@ int blastgpu_dposv_mixed_batched(const blastgpu_posv_desc* desc, int64_t batch, 
                                  void* workspace, double tol, int max_iter, int32_t* info,
                                  int32_t* iters, double* berr, blastgpu_stream_t stream);
 
+/* Allocation-free variant of blastgpu_dposv_mixed_batched (no counterpart in the reference: BLAST
+ * allocates nothing because it keeps its work in registers). For callers that cannot allocate
+ * device memory when they solve: a model-predictive controller calling the solver from its
+ * control loop, where allocation is ruled out after start-up because its latency is unbounded,
+ * or a host application that owns every device allocation. The binary32 factors go to a fixed
+ * scratch array inside the library's device memory instead of caller workspace:
+ *   - capacity BLASTGPU_NOALLOC_SCRATCH_BYTES = 32 MiB, reserved on every GPU that loads the
+ *     library until the process exits;
+ *   - scratch_bytes states the bytes the descriptors' ws_offset ranges use (max over instances
+ *     of ws_offset + blastgpu_dposv_mixed_workspace_bytes(n)); larger than the capacity returns
+ *     BLASTGPU_ERR_TOO_LARGE and launches nothing;
+ *   - the first call on a device looks up the array's device address (cudaGetSymbolAddress) and
+ *     caches it; make that first call before any stream capture;
+ *   - every call reuses the same array (nothing in it needs clearing: each factor is written
+ *     before it is read), so calls whose kernels overlap on the GPU race: serialise them.
+ * No cudaMalloc, cudaFree or allocating library routine is called. Results equal
+ * blastgpu_dposv_mixed_batched's. */
+#define BLASTGPU_NOALLOC_SCRATCH_BYTES ((size_t)32 << 20)
+int blastgpu_dposv_mixed_batched_noalloc(const blastgpu_posv_desc* desc, int64_t batch, int max_n,
+                                         size_t scratch_bytes, double tol, int max_iter, int32_t* info,
+                                         int32_t* iters, double* berr, blastgpu_stream_t stream);
+
 /* ---------------------------------------------------------------------------------------------
  * Adjoints (no BLAST counterpart). For X = A^{-1} B with A SPD and a scalar loss l:
  *   dl/dB = A^{-1} dl/dX,   dl/dA = -(dl/dB X^T + X dl/dB^T) / 2  (symmetrised),
