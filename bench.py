@@ -445,6 +445,57 @@ def workload_gemm24(args):
             "tflops": flops / ms / 1e9, "cpu_port_matrices_per_s": cpu, "cpu_threads": orc.max_threads()}
 
 
+def workload_riccati(args):
+    """BLAST's Riccati kernel (bench/blas/SyrkPotrf.cpp): D = chol(C + A^T*A), A 30 x 60, C 60 x 60
+    SPD, 50,000 instances; the fused kernel against syrkLower followed by potrf (two launches)."""
+    import numpy as np
+    import torch
+
+    import blast_gb300 as bg
+    from oracle import oracle as orc
+
+    batch, m, n = args.count or 50_000, 30, 60
+    g = torch.Generator(device="cuda")
+    g.manual_seed(7)
+    At = bg.col_major((batch,), m, n, "cuda")  # A (m x n), used as op(A) = A^T through .mT
+    At.copy_(torch.rand(batch, m, n, generator=g, device="cuda", dtype=torch.float64))
+    A = At.mT
+    Acol = bg.col_major((batch,), n, m, "cuda")
+    Acol.copy_(A)
+    G = torch.rand(batch, n, n, generator=g, device="cuda", dtype=torch.float64)
+    C = bg.col_major((batch,), n, n, "cuda")
+    C.copy_(G @ G.mT + n * torch.eye(n, device="cuda", dtype=torch.float64))
+    del G
+    D, S = bg.col_major((batch,), n, n, "cuda"), bg.col_major((batch,), n, n, "cuda")
+    fused = _timed(lambda: bg.syrk_potrf(1.0, A, 1.0, C, D), args.steps)
+
+    def composed():
+        bg.syrk_lower(1.0, Acol, 1.0, C, S)
+        bg.potrf(S, S)
+
+    comp = _timed(composed, args.steps)
+    torch.cuda.synchronize()
+    same = bool(torch.equal(torch.tril(D), torch.tril(S)))
+    flops = n * (n + 1) * m + n ** 3 / 3 + n ** 2 / 2 + n / 6
+    # CPU: the oracle's syrkLower then potrf, one instance per call, one thread
+    hA, hC = Acol[:256].cpu().numpy(), C[:256].cpu().numpy()
+    F = np.asfortranarray
+    t0 = time.perf_counter()
+    done = 0
+    while time.perf_counter() - t0 < 2.0:
+        for b in range(len(hA)):
+            Sb = F(np.zeros((n, n)))
+            orc.syrk_lower(1.0, F(hA[b]), 1.0, F(hC[b]), Sb)
+            orc.potrf(Sb, Sb)
+        done += len(hA)
+    cpu = done / (time.perf_counter() - t0)
+    return {"workload": f"syrk+potrf (Riccati) {batch} x D = chol(C + A^T A), A {m}x{n}",
+            "fused_ms": fused, "fused_matrices_per_s": batch / fused * 1e3,
+            "fused_tflops": flops * batch / fused / 1e9, "composed_ms": comp,
+            "composed_matrices_per_s": batch / comp * 1e3, "bitwise_equal": same,
+            "cpu_port_matrices_per_s_1thread": cpu}
+
+
 def workload_lu_ragged(args):
     """20,000 general matrices, n log-uniform in [4, 256], N(0,1), one RHS: getrf + getrs."""
     import numpy as np
@@ -542,7 +593,7 @@ def main():
     ap.add_argument("--batch", type=int, default=BATCH, help="matrices per GPU (default 50,000)")
     ap.add_argument("--no-mixed", action="store_true",
                     help="skip the FP64-vs-mixed comparison on the ragged n in [64, 512] batch")
-    ap.add_argument("--workload", choices=["cholesky48", "gemm24", "lu_ragged", "adjoint"],
+    ap.add_argument("--workload", choices=["cholesky48", "gemm24", "lu_ragged", "adjoint", "riccati"],
                     default="cholesky48", help="cholesky48 (default) prints the contract line; the "
                     "others print one JSON object for that workload")
     ap.add_argument("--count", type=int, default=0,
@@ -560,7 +611,8 @@ def main():
         import torch
 
         torch.cuda.set_device(0)
-        fn = {"gemm24": workload_gemm24, "lu_ragged": workload_lu_ragged, "adjoint": workload_adjoint}
+        fn = {"gemm24": workload_gemm24, "lu_ragged": workload_lu_ragged, "adjoint": workload_adjoint,
+              "riccati": workload_riccati}
         print(json.dumps(fn[args.workload](args)), flush=True)
     elif args.only_mixed:
         run_mixed_only(args)

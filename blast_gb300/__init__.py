@@ -5,11 +5,13 @@ build script, a ctypes binding, and ``blast``, a Python mirror of BLAST's functi
 torch device tensors.
 """
 from . import _lib
-from .blast import (LEFT, LOWER, RIGHT, UPPER, col_major, gemm, getrf, getrs, posv, potrf, potrs,
-                    syrk_lower, trmm, trsm)
+from .blast import (LEFT, LOWER, RIGHT, UPPER, col_major, gemm, ger, getrf, getrs, iamax, laswp,
+                    posv, potrf, potrs, swap, syrk_lower, syrk_potrf, trmm, trsm, trsv_left_lower,
+                    trsv_left_upper)
 
-__all__ = ["gemm", "potrf", "posv", "potrs", "getrf", "getrs", "syrk_lower", "trsm", "trmm",
-           "col_major", "LOWER", "UPPER", "LEFT", "RIGHT", "_lib"]
+__all__ = ["gemm", "potrf", "posv", "potrs", "getrf", "getrs", "syrk_lower", "syrk_potrf", "trsm", "trmm", "ger",
+           "iamax", "laswp", "swap", "trsv_left_lower", "trsv_left_upper", "col_major", "LOWER",
+           "UPPER", "LEFT", "RIGHT", "_lib"]
 
 
 def _apply_tuning():

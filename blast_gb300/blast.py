@@ -227,6 +227,29 @@ def syrk_lower(alpha, A: torch.Tensor, beta, C: torch.Tensor, D: torch.Tensor) -
     return D
 
 
+def syrk_potrf(alpha, A: torch.Tensor, beta, C: torch.Tensor, D: torch.Tensor) -> torch.Tensor:
+    """D = chol(beta*C + alpha*A*A^T), lower, fused (syrkLower then potrf: dense/Syrk.hpp:15-145,
+    dense/Potrf.hpp:66-106; BLAST's Riccati benchmark bench/blas/SyrkPotrf.cpp:15-40).
+
+    A is n x k, column-major, or a row-major tensor (BLAST's trans() view: op(A) = A^T of a k x n
+    matrix). Reads the lower triangle of C; D may be C. Returns the per-instance info.
+    """
+    a, c, d = _as_mat(A, "A"), _as_mat(C, "C"), _as_mat(D, "D")
+    n, k = a.rows, a.cols
+    if c.rows != n or c.cols != n or d.rows != n or d.cols != n:
+        raise ValueError("Matrix sizes do not match")
+    _square_col(c, "C")
+    _square_col(d, "D")
+    batch = _batch_of(a, c, d)
+    if d.batch != batch:
+        raise ValueError("D must hold the whole batch")
+    info = _info_tensor(batch, D.device)
+    _lib.call("blastgpu_dsyrk_potrf_strided", n, k, int(a.layout == ROW), float(alpha), a.ptr, a.ld,
+              _bstride(a, batch), float(beta), c.ptr, c.ld, _bstride(c, batch), d.ptr, d.ld, d.bstride,
+              info.data_ptr(), batch, _stream())
+    return info
+
+
 def trsm(uplo: int, unit: bool, A: torch.Tensor, B: torch.Tensor, X: torch.Tensor) -> torch.Tensor:
     """Solve A*X = B, A triangular (blast::trsm<UpLo, UNIT>(A, B, X), dense/Trsm.hpp:17-66).
 
@@ -276,6 +299,83 @@ def trmm(alpha, *args) -> torch.Tensor:
     if st != 0:
         raise _lib.BlastGpuError("blastgpu_dtrmm_strided", st)
     return C
+
+
+def _vec(v: torch.Tensor, name: str):
+    """(batch, n) or (n,) float64 CUDA tensor -> (ptr, n, inc, batch, batch stride)."""
+    if v.dtype != torch.float64 or not v.is_cuda:
+        raise TypeError(f"{name} must be a float64 CUDA tensor")
+    if v.dim() == 1:
+        return v.data_ptr(), v.shape[0], v.stride(0), 1, 0
+    if v.dim() == 2:
+        return v.data_ptr(), v.shape[1], v.stride(1), v.shape[0], v.stride(0)
+    raise ValueError(f"{name} must have shape (n,) or (batch, n)")
+
+
+def ger(alpha, x: torch.Tensor, y: torch.Tensor, A: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
+    """B = A + alpha*x*y^T (blast::ger, dense/Ger.hpp:40-135); B may be A."""
+    xp, m, incx, bx, sx = _vec(x, "x")
+    yp, n, incy, by, sy = _vec(y, "y")
+    a, bm = _as_mat(A, "A"), _as_mat(B, "B")
+    if a.rows != m or a.cols != n or bm.rows != m or bm.cols != n:
+        raise ValueError("Matrix sizes do not match")
+    _square_col(a, "A")
+    _square_col(bm, "B")
+    batch = max(bx, by, a.batch, bm.batch)
+    for cnt in (bx, by, a.batch):
+        if cnt not in (1, batch):
+            raise ValueError("Batch sizes do not match")
+    if bm.batch != batch:
+        raise ValueError("B must hold the whole batch")
+    _lib.call("blastgpu_dger_strided", m, n, float(alpha), xp, incx, sx if bx == batch else 0, yp, incy,
+              sy if by == batch else 0, a.ptr, a.ld, _bstride(a, batch), bm.ptr, bm.ld, bm.bstride, batch,
+              _stream())
+    return B
+
+
+def iamax(x: torch.Tensor) -> torch.Tensor:
+    """First index of the largest |x_i| per vector (blast::iamax, dense/Iamax.hpp:66-96)."""
+    xp, n, inc, batch, sx = _vec(x, "x")
+    if n == 0:
+        raise ValueError("Vector must be non-empty")
+    out = torch.empty(batch, dtype=torch.int32, device=x.device)
+    _lib.call("blastgpu_idamax_strided", n, xp, inc, sx, out.data_ptr(), batch, _stream())
+    return out
+
+
+def laswp(A: torch.Tensor, k0: int, k1: int, ipiv: torch.Tensor) -> torch.Tensor:
+    """Row interchanges k = k0..k1-1 with ipiv (blast::laswp, dense/Laswp.hpp:37-43), in place."""
+    a = _as_mat(A, "A")
+    _square_col(a, "A")
+    if ipiv.dtype != torch.int32 or not ipiv.is_cuda:
+        raise TypeError("ipiv must be an int32 CUDA tensor")
+    if ipiv.dim() == 2 and ipiv.shape[0] != a.batch:
+        raise ValueError("Batch sizes do not match")
+    if ipiv.shape[-1] < k1 or ipiv.stride(-1) != 1:
+        raise ValueError("ipiv must be contiguous and hold k1 pivots")
+    sp = ipiv.stride(0) if ipiv.dim() == 2 else 0
+    _lib.call("blastgpu_dlaswp_strided", a.cols, a.ptr, a.ld, a.bstride, int(k0), int(k1), ipiv.data_ptr(),
+              sp, a.batch, _stream())
+    return A
+
+
+def swap(x: torch.Tensor, y: torch.Tensor):
+    """Exchange two vectors (blast::swap, dense/Swap.hpp:35-44)."""
+    xp, n, incx, bx, sx = _vec(x, "x")
+    yp, n2, incy, by, sy = _vec(y, "y")
+    if n != n2 or bx != by:
+        raise ValueError("Vector sizes must be equal")
+    _lib.call("blastgpu_dswap_strided", n, xp, incx, sx, yp, incy, sy, bx, _stream())
+
+
+def trsv_left_lower(A: torch.Tensor, b: torch.Tensor, x: torch.Tensor) -> torch.Tensor:
+    """Solve A*x = b, A lower triangular (blast::trsvLeftLower, dense/Trsv.hpp:15-38)."""
+    return trsm(LOWER, False, A, b.unsqueeze(-1), x.unsqueeze(-1)).squeeze(-1)
+
+
+def trsv_left_upper(A: torch.Tensor, b: torch.Tensor, x: torch.Tensor) -> torch.Tensor:
+    """Solve A*x = b, A upper triangular (blast::trsvLeftUpper, dense/Trsv.hpp:41-68)."""
+    return trsm(UPPER, False, A, b.unsqueeze(-1), x.unsqueeze(-1)).squeeze(-1)
 
 
 def col_major(batch_shape, rows: int, cols: int, device="cuda", ld: int | None = None) -> torch.Tensor:

@@ -40,19 +40,69 @@ struct PanelAddr {
     }
 };
 
+// Sources of the matrix being factorised; fill() loads the KM x KN tile at (i, k).
+// LoadSrc: the input matrix A itself (blast::potrf(A, L)).
+template <class Addr>
+struct LoadSrc {
+    const double* A;
+    Addr ia;
+    template <int KM, int KN, bool DIAG>
+    __device__ __forceinline__ void fill(double (&acc)[KM][KN], int n, int k, int i, int nc) const {
+#pragma unroll
+        for (int c = 0; c < KN; ++c)
+#pragma unroll
+            for (int r = 0; r < KM; ++r)
+                acc[r][c] = (c < nc && i + r < n) ? A[ia(i + r, k + c)] : 0.0;
+    }
+};
+
+// SyrkSrc: beta*C + alpha*A*A^T (A: n x K, or K x n read transposed), formed tile by tile in the
+// order of blast::syrkLower (dense/Syrk.hpp:15-145): v = beta*c_ij rounded (RegisterMatrix::load(
+// beta, ..)), then for l ascending v = fma(alpha*a_il, a_jl, v) (RegisterMatrix::ger(alpha, ..)).
+// The factorisation then runs on exactly the values syrkLower would have stored.
+struct SyrkSrc {
+    const double* A;
+    int64_t lda;
+    int K;
+    bool trans;
+    double alpha, beta;
+    const double* C;
+    int64_t ldc;
+    __device__ __forceinline__ double a(int i, int l) const {
+        return trans ? A[l + (int64_t)i * lda] : A[i + (int64_t)l * lda];
+    }
+    template <int KM, int KN, bool DIAG>
+    __device__ __forceinline__ void fill(double (&acc)[KM][KN], int n, int k, int i, int nc) const {
+#pragma unroll
+        for (int c = 0; c < KN; ++c)
+#pragma unroll
+            for (int r = 0; r < KM; ++r)
+                acc[r][c] = (c < nc && i + r < n && (!DIAG || r >= c)) ? beta * C[(i + r) + (int64_t)(k + c) * ldc]
+                                                                      : 0.0;
+        for (int l = 0; l < K; ++l) {
+            double ax[KM], b[KN];
+#pragma unroll
+            for (int r = 0; r < KM; ++r) ax[r] = (i + r < n) ? alpha * a(i + r, l) : 0.0;
+#pragma unroll
+            for (int c = 0; c < KN; ++c) b[c] = (c < nc) ? a(k + c, l) : 0.0;
+#pragma unroll
+            for (int c = 0; c < KN; ++c)
+#pragma unroll
+                for (int r = 0; r < KM; ++r)
+                    if (!DIAG || r >= c) acc[r][c] = fma(ax[r], b[c], acc[r][c]);
+        }
+    }
+};
+
 // One KM x KN register tile of the left-looking strip k (rows i .. i+KM-1). DIAG: the strip's
 // first tile, which holds the diagonal block; its strictly upper entries (r < c) are never stored,
 // so their fused multiply-adds are left out at compile time.
-template <int KM, int KN, bool DIAG, class Addr>
-__device__ __forceinline__ void potrf_tile(int n, int k, int i, int nc, const double* A, Addr ia,
-                                           double* L, Addr il, double (&y)[KN], int& info) {
+template <int KM, int KN, bool DIAG, class Src, class Addr>
+__device__ __forceinline__ void potrf_tile(int n, int k, int i, int nc, Src const& src, double* L, Addr il,
+                                           double (&y)[KN], int& info) {
     constexpr bool diag = DIAG;
     double acc[KM][KN];
-#pragma unroll
-    for (int c = 0; c < KN; ++c)
-#pragma unroll
-        for (int r = 0; r < KM; ++r)
-            acc[r][c] = (c < nc && i + r < n) ? A[ia(i + r, k + c)] : 0.0;
+    src.template fill<KM, KN, DIAG>(acc, n, k, i, nc);
 
     // acc -= L(i:i+KM, 0:k) * L(k:k+KN, 0:k)^T, one fused rank-1 update per column l
     // (BLAST's ger(-1, ...) loop, dense/Potrf.hpp:40-41).
@@ -120,8 +170,8 @@ __device__ __forceinline__ void potrf_tile(int n, int k, int i, int nc, const do
 // Left-looking Cholesky of one n x n matrix, strips of KN columns, row tiles of 3, 2 and 1 times
 // TS rows (dense: KN = TS = 4, dense/Potrf.hpp:87-105; panel: KN = min((RC-4)/3, SS), TS = SS,
 // panel/Potrf.hpp:84-105). Returns info (0 or first bad pivot + 1).
-template <int KN, int TS, class Addr>
-__device__ int potrf_thread(int n, const double* A, Addr ia, double* L, Addr il) {
+template <int KN, int TS, class Src, class Addr>
+__device__ int potrf_thread_src(int n, Src const& A, double* L, Addr il) {
     int info = 0;
     for (int k = 0; k < n; k += KN) {
         int const nc = min(KN, n - k);
@@ -133,21 +183,26 @@ __device__ int potrf_thread(int n, const double* A, Addr ia, double* L, Addr il)
             // than TS remain, then TS.
             bool const first = i == k;
             if (rem > 2 * TS) {
-                if (first) potrf_tile<3 * TS, KN, true>(n, k, i, nc, A, ia, L, il, y, info);
-                else potrf_tile<3 * TS, KN, false>(n, k, i, nc, A, ia, L, il, y, info);
+                if (first) potrf_tile<3 * TS, KN, true>(n, k, i, nc, A, L, il, y, info);
+                else potrf_tile<3 * TS, KN, false>(n, k, i, nc, A, L, il, y, info);
                 i += 3 * TS;
             } else if (rem > TS) {
-                if (first) potrf_tile<2 * TS, KN, true>(n, k, i, nc, A, ia, L, il, y, info);
-                else potrf_tile<2 * TS, KN, false>(n, k, i, nc, A, ia, L, il, y, info);
+                if (first) potrf_tile<2 * TS, KN, true>(n, k, i, nc, A, L, il, y, info);
+                else potrf_tile<2 * TS, KN, false>(n, k, i, nc, A, L, il, y, info);
                 i += 2 * TS;
             } else {
-                if (first) potrf_tile<TS, KN, true>(n, k, i, nc, A, ia, L, il, y, info);
-                else potrf_tile<TS, KN, false>(n, k, i, nc, A, ia, L, il, y, info);
+                if (first) potrf_tile<TS, KN, true>(n, k, i, nc, A, L, il, y, info);
+                else potrf_tile<TS, KN, false>(n, k, i, nc, A, L, il, y, info);
                 i += TS;
             }
         }
     }
     return info;
+}
+
+template <int KN, int TS, class Addr>
+__device__ __forceinline__ int potrf_thread(int n, const double* A, Addr ia, double* L, Addr il) {
+    return potrf_thread_src<KN, TS>(n, LoadSrc<Addr>{A, ia}, L, il);
 }
 
 constexpr int kRhs = 8;  // right-hand sides per register block of the solves
@@ -298,6 +353,26 @@ __global__ void __launch_bounds__(32, 12) potrf_desc_kernel(const blastgpu_potrf
     if (info) info[b] = r;
 }
 
+// D = chol(beta*C + alpha*op(A)*op(A)^T), lower, one thread per instance: syrkLower's values are
+// formed inside the factorisation's register tiles and never stored.
+struct SyrkPotrfArgs {
+    int n, k, trans;
+    double alpha, beta;
+    const double* A; int lda; int64_t sa;
+    const double* C; int ldc; int64_t sc;
+    double* D; int ldd; int64_t sd;
+    int32_t* info;
+    int64_t batch;
+};
+
+__global__ void __launch_bounds__(32, 12) syrk_potrf_thread_kernel(SyrkPotrfArgs p) {
+    int64_t const b = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    if (b >= p.batch) return;
+    SyrkSrc const src{p.A + b * p.sa, p.lda, p.k, p.trans != 0, p.alpha, p.beta, p.C + b * p.sc, p.ldc};
+    int const info = potrf_thread_src<4, 4>(p.n, src, p.D + b * p.sd, ColAddr{p.ldd});
+    if (p.info) p.info[b] = info;
+}
+
 int launch_posv(PosvArgs const& p, cudaStream_t stream) {
     if (p.batch == 0 || p.n == 0) {
         if (p.info && p.batch > 0) {
@@ -396,6 +471,38 @@ int blastgpu_dpotrs_strided(int n, int nrhs, const double* L, int ldl, int64_t s
     PosvArgs p{n, nrhs, nullptr, 1, 0, const_cast<double*>(L), ldl, stride_l, B, ldb, stride_b, X, ldx,
                stride_x, nullptr, batch, 2};
     return launch_posv(p, as_cuda(stream));
+}
+
+int blastgpu_dsyrk_potrf_strided(int n, int k, int trans_a, double alpha, const double* A, int lda,
+                                 int64_t stride_a, double beta, const double* C, int ldc, int64_t stride_c,
+                                 double* D, int ldd, int64_t stride_d, int32_t* info, int64_t batch,
+                                 blastgpu_stream_t stream) {
+    if (n < 0) return -1;
+    if (k < 0) return -2;
+    if (trans_a != 0 && trans_a != 1) return -3;
+    int const arows = trans_a ? k : n;
+    if (n > 0 && k > 0 && !A) return -5;
+    if (lda < (arows > 0 ? arows : 1)) return -6;
+    if (n > 0 && !C) return -9;
+    if (ldc < (n > 0 ? n : 1)) return -10;
+    if (n > 0 && !D) return -12;
+    if (ldd < (n > 0 ? n : 1)) return -13;
+    if (batch < 0) return -16;
+    cudaStream_t const s = as_cuda(stream);
+    if (batch == 0) return BLASTGPU_SUCCESS;
+    if (n == 0) {
+        if (info) {
+            cudaError_t const e = cudaMemsetAsync(info, 0, sizeof(int32_t) * batch, s);
+            if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
+        }
+        return BLASTGPU_SUCCESS;
+    }
+    int64_t const blocks = (batch + 31) / 32;
+    if (blocks > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
+    SyrkPotrfArgs const p{n, k, trans_a, alpha, beta, A, lda, stride_a, C, ldc, stride_c, D, ldd, stride_d, info,
+                          batch};
+    syrk_potrf_thread_kernel<<<(unsigned)blocks, 32, 0, s>>>(p);
+    return check_launch();
 }
 
 }  // extern "C"

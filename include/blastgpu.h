@@ -90,6 +90,39 @@ int blastgpu_tune_get(const char* key, int* value);
 int blastgpu_selftest_recip(int which, const double* x, double* y, int n, blastgpu_stream_t stream);
 int blastgpu_probe_fp64_tflops(double* tflops, blastgpu_stream_t stream);
 
+/* D = chol(beta*C + alpha*op(A)*op(A)^T), lower triangle; op(A) = A (n x k) or, with trans_a = 1,
+ * the transpose of a k x n A. The Riccati-recursion kernel that BLAST benchmarks as syrk followed
+ * by potrf (bench/blas/SyrkPotrf.cpp:15-40; BLASFEO's dsyrk_dpotrf_ln,
+ * include/blasfeo/blasfeo_api/SyrkPotrf.hpp:15-40), fused: the values of syrkLower
+ * (dense/Syrk.hpp:15-145) are formed in the factorisation's register tiles, so the result equals
+ * blastgpu_dsyrk_lower_strided then blastgpu_dpotrf_strided bit for bit without storing the sum.
+ * Reads only the lower triangle of C; D may alias C, not A. info[b] as blastgpu_dpotrf_strided. */
+int blastgpu_dsyrk_potrf_strided(int n, int k, int trans_a, double alpha, const double* A, int lda,
+                                 int64_t stride_a, double beta, const double* C, int ldc, int64_t stride_c,
+                                 double* D, int ldd, int64_t stride_d, int32_t* info, int64_t batch,
+                                 blastgpu_stream_t stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * BLAS-2 building blocks of BLAST's LU, batched (uniform batches; vectors with increments).
+ *   ger:   B = A + alpha*x*y^T, b_ij = fma(alpha*x_i, y_j, a_ij)   (blast::ger, dense/Ger.hpp:40-135);
+ *          B may equal A.
+ *   iamax: result[b] = first index of the largest |x_i|            (blast::iamax, dense/Iamax.hpp:66-96)
+ *   laswp: swap rows k and ipiv[k] of A's ncols columns, k = k0..k1-1 (blast::laswp, dense/Laswp.hpp:37-43)
+ *   swap:  exchange vectors x and y                                (blast::swap, dense/Swap.hpp:35-44)
+ * trsvLeftLower / trsvLeftUpper (dense/Trsv.hpp:15-68) are blastgpu_dtrsm_strided with n = 1.
+ * ------------------------------------------------------------------------------------------- */
+int blastgpu_dger_strided(int m, int n, double alpha, const double* x, int incx, int64_t stride_x,
+                          const double* y, int incy, int64_t stride_y, const double* A, int lda,
+                          int64_t stride_a, double* B, int ldb, int64_t stride_b, int64_t batch,
+                          blastgpu_stream_t stream);
+int blastgpu_idamax_strided(int n, const double* x, int incx, int64_t stride_x, int32_t* result,
+                            int64_t batch, blastgpu_stream_t stream);
+int blastgpu_dlaswp_strided(int ncols, double* A, int lda, int64_t stride_a, int k0, int k1,
+                            const int32_t* ipiv, int64_t stride_ipiv, int64_t batch,
+                            blastgpu_stream_t stream);
+int blastgpu_dswap_strided(int n, double* x, int incx, int64_t stride_x, double* y, int incy,
+                           int64_t stride_y, int64_t batch, blastgpu_stream_t stream);
+
 /* ---------------------------------------------------------------------------------------------
  * Layout conversion: dst = src element by element, for any pair of layouts (column-major,
  * row-major, panel of height ps). Replaces BLAST's assign() between panel and dense matrices

@@ -177,6 +177,89 @@ inline void getrf(Batch const& A, std::int32_t* ipiv, std::int64_t ipiv_stride, 
                   "getrf");
 }
 
+// ---- BLAS-2 building blocks ------------------------------------------------------------------
+// A vector: size elements at data[i*inc]; a batch of vectors repeats it every `stride` doubles.
+struct Vector {
+    double* data;
+    int size;
+    int inc;
+};
+inline Vector vector(double* data, int size, int inc = 1) { return Vector{data, size, inc}; }
+struct VectorBatch {
+    Vector first;
+    std::int64_t stride;  // doubles between consecutive instances (0: one vector shared by all)
+    std::int64_t count;
+};
+inline VectorBatch batch(Vector v) { return VectorBatch{v, 0, 1}; }
+
+namespace detail {
+inline std::int64_t vstride_for(VectorBatch const& b, std::int64_t n) { return b.count == n ? b.stride : 0; }
+inline std::int64_t max_count(std::initializer_list<std::int64_t> cs) {
+    std::int64_t n = 1;
+    for (auto c : cs) n = c > n ? c : n;
+    for (auto c : cs)
+        if (c != 1 && c != n) throw std::invalid_argument("Batch sizes do not match");
+    return n;
+}
+inline Batch as_column(VectorBatch const& v) {
+    if (v.first.inc != 1) throw std::logic_error("trsv needs unit-stride vectors");
+    return Batch{Matrix{v.first.data, v.first.size, 1, v.first.size > 0 ? v.first.size : 1, false}, v.stride,
+                 v.count};
+}
+}  // namespace detail
+
+// B = A + alpha*x*y^T (blast::ger, dense/Ger.hpp:40-135); B may be A.
+inline void ger(double alpha, VectorBatch const& x, VectorBatch const& y, Batch const& A, Batch const& B,
+                blastgpu_stream_t stream = nullptr) {
+    int const M = x.first.size, N = y.first.size;
+    if (A.first.rows != M || A.first.cols != N || B.first.rows != M || B.first.cols != N)
+        throw std::invalid_argument("Matrix sizes do not match");
+    if (A.first.row_major || B.first.row_major) throw std::logic_error("ger needs column-major storage");
+    std::int64_t const n = detail::max_count({x.count, y.count, A.count, B.count});
+    if (B.count != n) throw std::invalid_argument("B must hold the whole batch");
+    detail::check(blastgpu_dger_strided(M, N, alpha, x.first.data, x.first.inc, detail::vstride_for(x, n),
+                                        y.first.data, y.first.inc, detail::vstride_for(y, n), A.first.data,
+                                        A.first.ld, detail::stride_for(A, n), B.first.data, B.first.ld, B.stride,
+                                        n, stream),
+                  "ger");
+}
+
+// result[b] = first index of the largest |x_i| (blast::iamax, dense/Iamax.hpp:66-96); device int32.
+inline void iamax(VectorBatch const& x, std::int32_t* result, blastgpu_stream_t stream = nullptr) {
+    if (x.first.size <= 0) throw std::invalid_argument("Vector must be non-empty");
+    detail::check(blastgpu_idamax_strided(x.first.size, x.first.data, x.first.inc, x.stride, result, x.count,
+                                          stream),
+                  "iamax");
+}
+
+// Rows k and ipiv[k] of A exchanged for k = k0..k1-1 (blast::laswp, dense/Laswp.hpp:37-43).
+inline void laswp(Batch const& A, int k0, int k1, std::int32_t const* ipiv, std::int64_t ipiv_stride,
+                  blastgpu_stream_t stream = nullptr) {
+    if (A.first.row_major) throw std::logic_error("laswp needs column-major storage");
+    detail::check(blastgpu_dlaswp_strided(A.first.cols, A.first.data, A.first.ld, A.stride, k0, k1, ipiv,
+                                          ipiv_stride, A.count, stream),
+                  "laswp");
+}
+
+// Exchanges x and y (blast::swap, dense/Swap.hpp:35-44).
+inline void swap(VectorBatch const& x, VectorBatch const& y, blastgpu_stream_t stream = nullptr) {
+    if (x.first.size != y.first.size || x.count != y.count) throw std::invalid_argument("Vector sizes must be equal");
+    detail::check(blastgpu_dswap_strided(x.first.size, x.first.data, x.first.inc, x.stride, y.first.data,
+                                         y.first.inc, y.stride, x.count, stream),
+                  "swap");
+}
+
+// Solve A*x = b, A lower / upper triangular (blast::trsvLeftLower / trsvLeftUpper,
+// dense/Trsv.hpp:15-68): trsm with one right-hand side, the same operation order.
+inline void trsvLeftLower(Batch const& A, VectorBatch const& b, VectorBatch const& x,
+                          blastgpu_stream_t stream = nullptr) {
+    trsm<UpLo::Lower, false>(A, detail::as_column(b), detail::as_column(x), stream);
+}
+inline void trsvLeftUpper(Batch const& A, VectorBatch const& b, VectorBatch const& x,
+                          blastgpu_stream_t stream = nullptr) {
+    trsm<UpLo::Upper, false>(A, detail::as_column(b), detail::as_column(x), stream);
+}
+
 // Throws what BLAST's getf2 throws for a singular pivot (dense/Getf2.hpp:68-69), given the
 // per-instance info copied to the host.
 inline void check_singular(std::int32_t const* info_host, std::int64_t count) {

@@ -537,6 +537,18 @@ int oracle_idamax(int n, const double* x, int incx) {
     return index;
 }
 
+int oracle_dger(double alpha, const double* x, int incx, const double* y, int incy, oracle_mat A,
+                oracle_mat B) {
+    if (!valid(A)) return -6;
+    if (!valid(B) || B.rows != A.rows || B.cols != A.cols) return -7;
+    Gen a(A), b(B);
+    for (int j = 0; j < A.cols; ++j) {
+        double const yj = y[(int64_t)j * incy];
+        for (int i = 0; i < A.rows; ++i) b(i, j) = std::fma(alpha * x[(int64_t)i * incx], yj, a(i, j));
+    }
+    return 0;
+}
+
 int oracle_dtrsm(int uplo, int unit, int trans_a, oracle_mat A, oracle_mat B, oracle_mat X) {
     if (!valid(A)) return -4;
     if (!valid(B)) return -5;

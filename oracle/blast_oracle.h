@@ -71,6 +71,11 @@ void oracle_dlaswp(oracle_mat A, int k0, int k1, const int32_t* ipiv);
 /* First index of max |x| (dense/Iamax.hpp:82-95). */
 int oracle_idamax(int n, const double* x, int incx);
 
+/* blast::ger (dense/Ger.hpp:40-135 with RegisterMatrix::ger, register_matrix/RegisterMatrix.hpp:
+ * 610-628): b_ij = fma(alpha*x_i, y_j, a_ij), alpha*x_i rounded first. B may alias A. */
+int oracle_dger(double alpha, const double* x, int incx, const double* y, int incy, oracle_mat A,
+                oracle_mat B);
+
 /* Left triangular solve A*X = B, uplo 0 lower / 1 upper, unit 0/1; X may alias B
  * (dense/Trsm.hpp:17-66). trans_a=1 solves with A^T (BLAST's trans() view). */
 int oracle_dtrsm(int uplo, int unit, int trans_a, oracle_mat A, oracle_mat B, oracle_mat X);

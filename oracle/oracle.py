@@ -48,6 +48,7 @@ def lib() -> C.CDLL:
             "oracle_dgetf2": [M, P],
             "oracle_dlaswp": [M, I, I, P],
             "oracle_idamax": [I, P, I],
+            "oracle_dger": [D, P, I, P, I, M, M],
             "oracle_dtrsm": [I, I, I, M, M, M],
             "oracle_dtrmm": [I, I, I, D, M, M, M],
             "oracle_dpotrs": [M, M, M],
@@ -123,6 +124,20 @@ def laswp(A, k0, k1, ipiv):
 def idamax(x) -> int:
     x = np.ascontiguousarray(x, dtype=np.float64)
     return lib().oracle_idamax(len(x), x.ctypes.data, 1)
+
+
+def ger(alpha, x, y, A, B):
+    """B = A + alpha*x*y^T in place into B (blast::ger, dense/Ger.hpp:40-135)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    return _check(lib().oracle_dger(alpha, x.ctypes.data, 1, y.ctypes.data, 1, mat(A), mat(B)), "ger")
+
+
+def swap(x, y):
+    """blast::swap (dense/Swap.hpp:35-44): exchanges the contents of two vectors."""
+    t = x.copy()
+    x[...] = y
+    y[...] = t
 
 
 def trsm(uplo: int, unit: int, A, B, X, trans_a: int = 0):

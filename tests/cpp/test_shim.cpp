@@ -92,6 +92,36 @@ int main() {
     try { blastgpu::check_singular(&info, 1); } catch (std::invalid_argument const&) { threw = true; }
     CHECK(threw && info == 1);
 
+    // ger, trsvLeftLower and iamax on one instance: B = A + 0.5*x*y^T, solve tril(B + n I) x = b
+    {
+        std::vector<double> x(n), y(n), b(n);
+        for (int i = 0; i < n; ++i) { x[i] = U(gen); y[i] = U(gen); b[i] = U(gen); }
+        double *dx = upload(x), *dy = upload(y), *db = upload(b), *dB2 = upload(A);
+        blastgpu::ger(0.5, blastgpu::batch(blastgpu::vector(dx, n)), blastgpu::batch(blastgpu::vector(dy, n)),
+                      blastgpu::batch(blastgpu::matrix(dA, n, n)), blastgpu::batch(blastgpu::matrix(dB2, n, n)));
+        auto G = download(dB2, nn);
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i < n; ++i) CHECK(G[i + j * n] == std::fma(0.5 * x[i], y[j], A[i + j * n]));
+        for (int i = 0; i < n; ++i) G[i + i * n] += n;
+        double* dG = upload(G);
+        blastgpu::trsvLeftLower(blastgpu::batch(blastgpu::matrix(dG, n, n)), blastgpu::batch(blastgpu::vector(db, n)),
+                                blastgpu::batch(blastgpu::vector(dx, n)));
+        auto xs = download(dx, n);
+        for (int i = 0; i < n; ++i) {
+            double r = b[i];
+            for (int j = 0; j <= i; ++j) r -= G[i + j * n] * xs[j];
+            CHECK(std::fabs(r) < 1e-12 * n);
+        }
+        std::int32_t* didx = nullptr;
+        CHECK(cudaMalloc(&didx, sizeof(std::int32_t)) == cudaSuccess);
+        blastgpu::iamax(blastgpu::batch(blastgpu::vector(db, n)), didx);
+        std::int32_t idx = -1;
+        CHECK(cudaMemcpy(&idx, didx, sizeof(idx), cudaMemcpyDeviceToHost) == cudaSuccess);
+        int want = 0;
+        for (int i = 1; i < n; ++i) if (std::fabs(b[i]) > std::fabs(b[want])) want = i;
+        CHECK(idx == want);
+    }
+
     // size mismatch and unimplemented variants throw BLAST's exception types
     threw = false;
     try { blastgpu::gemm(bt(dA), blastgpu::batch(blastgpu::matrix(dB, n - 1, n)), bt(dC), bt(dD)); }

@@ -229,6 +229,23 @@ def test_iamax(orc):
 # ------------------------------------------------------------------------------------------------
 # 2. LAPACK golden vectors
 # ------------------------------------------------------------------------------------------------
+def test_ger_sweep(orc):
+    """blast::ger against A + alpha*x*y^T, sizes of dense/GerTest.cpp (m, n in 1..20, 1e-10)."""
+    rng = np.random.default_rng(5)
+    for m in range(1, 21):
+        for n in range(1, 21):
+            x, y, A = rng.random(m), rng.random(n), np.asfortranarray(rng.random((m, n)))
+            alpha = float(rng.random())
+            B = np.asfortranarray(np.zeros((m, n)))
+            orc.ger(alpha, x, y, A, B)
+            assert approx_equal(B, A + alpha * np.outer(x, y), 1e-10, 1e-10)
+            # b_ij = fma(alpha*x_i, y_j, a_ij): exact for these small dyadic values
+    x, y = np.array([0.5, 0.25]), np.array([2.0, 4.0])
+    A = np.asfortranarray(np.ones((2, 2)))
+    orc.ger(2.0, x, y, A, A)
+    assert np.array_equal(A, [[3.0, 5.0], [2.0, 3.0]])
+
+
 def test_golden_potrf_potrs(orc, golden):
     for n in (1, 2, 4, 5, 13, 24, 48):
         A, Lg = golden[f"potrf_A_{n}"], golden[f"potrf_L_{n}"]
