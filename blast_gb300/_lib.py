@@ -61,6 +61,8 @@ SIGNATURES: dict[str, list] = {
     "blastgpu_dpotrs_strided": [I32, I32, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, I64, PTR],
     "blastgpu_dpotrf_batched": [PTR, I64, I32, I32, PTR, PTR],
     "blastgpu_dcopy_batched": [PTR, I64, PTR, PTR],
+    "blastgpu_dposv_mirror_strided": [I32, I32, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64,
+                                      PTR, PTR, PTR, I64, PTR],
     "blastgpu_dsyrk_potrf_strided": [I32, I32, I32, DBL, PTR, I32, I64, DBL, PTR, I32, I64, PTR, I32, I64, PTR,
                                      I64, PTR],
     "blastgpu_dger_strided": [I32, I32, DBL, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, I64, PTR],

@@ -170,8 +170,13 @@ __device__ __forceinline__ void potrf_tile(int n, int k, int i, int nc, Src cons
 // Left-looking Cholesky of one n x n matrix, strips of KN columns, row tiles of 3, 2 and 1 times
 // TS rows (dense: KN = TS = 4, dense/Potrf.hpp:87-105; panel: KN = min((RC-4)/3, SS), TS = SS,
 // panel/Potrf.hpp:84-105). Returns info (0 or first bad pivot + 1).
-template <int KN, int TS, class Src, class Addr>
-__device__ int potrf_thread_src(int n, Src const& A, double* L, Addr il) {
+struct NoStripHook {
+    __device__ __forceinline__ void operator()(int, int) const {}
+};
+
+// after_strip(k, nc) runs once columns k .. k+nc-1 of L are final.
+template <int KN, int TS, class Src, class Addr, class Hook = NoStripHook>
+__device__ int potrf_thread_src(int n, Src const& A, double* L, Addr il, Hook const& after_strip = Hook{}) {
     int info = 0;
     for (int k = 0; k < n; k += KN) {
         int const nc = min(KN, n - k);
@@ -196,6 +201,7 @@ __device__ int potrf_thread_src(int n, Src const& A, double* L, Addr il) {
                 i += TS;
             }
         }
+        after_strip(k, nc);
     }
     return info;
 }
@@ -330,6 +336,76 @@ __global__ void __launch_bounds__(THREADS, MINB) posv_thread_kernel(PosvArgs p) 
         double* X = p.X + b * p.sx;
         trsm_lower_thread(p.n, p.nrhs, L, p.ldl, p.B + b * p.sb, p.ldb, X, p.ldx);
         trsm_lower_trans_thread(p.n, p.nrhs, L, p.ldl, X, p.ldx);
+    }
+}
+
+// Cholesky solve whose inputs and outputs may live in host memory the GPU addresses directly
+// (pinned, or any allocation on hardware-coherent systems). A and B are read once each, in place,
+// by the thread that owns the instance; the factorisation and the solves run on working copies in
+// the device workspaces p.L / p.X (ld = n), which they re-read. The warp copies its 32 instances'
+// final L columns out to the caller's Lh after every strip of 4 columns (lanes over rows, so the
+// host sees whole-line writes instead of one 8-byte store per thread, spread over the
+// factorisation), and X at the end. On GB300 these reads and writes cross NVLink-C2C while the
+// binary64 pipe computes.
+struct MirrorOut {
+    double* Lh; int ldlh; int64_t slh;
+    double* Xh; int ldxh; int64_t sxh;
+};
+
+// Copies rows j .. n-1 of columns j0 .. j0+nc-1 of `cnt` consecutive instances, one warp.
+__device__ __forceinline__ void warp_copy_lower_cols(int n, int j0, int nc, int cnt, const double* W, int ldw,
+                                                     int64_t sw, double* H, int ldh, int64_t sh, int lane) {
+    for (int m = 0; m < cnt; ++m)
+        for (int j = j0; j < j0 + nc; ++j)
+            for (int i = j + lane; i < n; i += 32)
+                H[m * sh + i + (int64_t)j * ldh] = W[m * sw + i + (int64_t)j * ldw];
+}
+
+struct StripCopyOut {
+    int n, cnt, lane;
+    const double* W; int ldw; int64_t sw;
+    double* H; int ldh; int64_t sh;
+    __device__ __forceinline__ void operator()(int k, int nc) const {
+        __syncwarp();
+        warp_copy_lower_cols(n, k, nc, cnt, W, ldw, sw, H, ldh, sh, lane);
+    }
+};
+
+__global__ void __launch_bounds__(32, 12) posv_mirror_kernel(PosvArgs p, MirrorOut o) {
+    int64_t const b0 = (int64_t)blockIdx.x * 32;
+    int const lane = threadIdx.x;
+    int64_t const b = b0 + lane;
+    int const n = p.n;
+    bool const full = b0 + 32 <= p.batch;  // warp-uniform
+    int const cnt = full ? 32 : (int)(p.batch - b0);
+    if (full) {  // L leaves strip by strip
+        double* L = p.L + b * p.sl;
+        StripCopyOut const out{n, 32, lane, p.L + b0 * p.sl, p.ldl, p.sl, o.Lh + b0 * o.slh, o.ldlh, o.slh};
+        int const info = potrf_thread_src<4, 4>(n, LoadSrc<ColAddr>{p.A + b * p.sa, ColAddr{p.lda}}, L,
+                                                ColAddr{p.ldl}, out);
+        if (p.info) p.info[b] = info;
+    } else if (b < p.batch) {
+        double* L = p.L + b * p.sl;
+        int const info = potrf_thread<4, 4>(n, p.A + b * p.sa, ColAddr{p.lda}, L, ColAddr{p.ldl});
+        if (p.info) p.info[b] = info;
+    }
+    if (b < p.batch) {
+        double* L = p.L + b * p.sl;
+        if (p.nrhs > 0) {
+            double* X = p.X + b * p.sx;
+            trsm_lower_thread(n, p.nrhs, L, p.ldl, p.B + b * p.sb, p.ldb, X, p.ldx);
+            trsm_lower_trans_thread(n, p.nrhs, L, p.ldl, X, p.ldx);
+        }
+    }
+    __syncwarp();
+    if (!full)
+        warp_copy_lower_cols(n, 0, n, cnt, p.L + b0 * p.sl, p.ldl, p.sl, o.Lh + b0 * o.slh, o.ldlh, o.slh, lane);
+    if (p.nrhs == 0) return;
+    for (int m = 0; m < cnt; ++m) {
+        const double* X = p.X + (b0 + m) * p.sx;
+        double* Xh = o.Xh + (b0 + m) * o.sxh;
+        for (int j = 0; j < p.nrhs; ++j)
+            for (int i = lane; i < n; i += 32) Xh[i + (int64_t)j * o.ldxh] = X[i + (int64_t)j * p.ldx];
     }
 }
 
@@ -471,6 +547,41 @@ int blastgpu_dpotrs_strided(int n, int nrhs, const double* L, int ldl, int64_t s
     PosvArgs p{n, nrhs, nullptr, 1, 0, const_cast<double*>(L), ldl, stride_l, B, ldb, stride_b, X, ldx,
                stride_x, nullptr, batch, 2};
     return launch_posv(p, as_cuda(stream));
+}
+
+int blastgpu_dposv_mirror_strided(int n, int nrhs, const double* A, int lda, int64_t stride_a,
+                                  const double* B, int ldb, int64_t stride_b, double* L, int ldl,
+                                  int64_t stride_l, double* X, int ldx, int64_t stride_x, double* L_work,
+                                  double* X_work, int32_t* info, int64_t batch, blastgpu_stream_t stream) {
+    if (n < 0) return -1;
+    if (nrhs < 0) return -2;
+    if (n > 0 && !A) return -3;
+    if (lda < (n > 0 ? n : 1)) return -4;
+    if (n > 0 && nrhs > 0 && !B) return -6;
+    if (ldb < (n > 0 ? n : 1)) return -7;
+    if (n > 0 && !L) return -9;
+    if (ldl < (n > 0 ? n : 1)) return -10;
+    if (n > 0 && nrhs > 0 && !X) return -12;
+    if (ldx < (n > 0 ? n : 1)) return -13;
+    if (n > 0 && !L_work) return -15;
+    if (n > 0 && nrhs > 0 && !X_work) return -16;
+    if (batch < 0) return -18;
+    cudaStream_t const s = as_cuda(stream);
+    if (batch == 0) return BLASTGPU_SUCCESS;
+    if (n == 0) {
+        if (info) {
+            cudaError_t const e = cudaMemsetAsync(info, 0, sizeof(int32_t) * batch, s);
+            if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
+        }
+        return BLASTGPU_SUCCESS;
+    }
+    int64_t const blocks = (batch + 31) / 32;
+    if (blocks > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
+    PosvArgs const p{n, nrhs, A, lda, stride_a, L_work, n, (int64_t)n * n, B, ldb, stride_b, X_work, n,
+                     (int64_t)n * nrhs, info, batch, 1};
+    MirrorOut const o{L, ldl, stride_l, X, ldx, stride_x};
+    posv_mirror_kernel<<<(unsigned)blocks, 32, 0, s>>>(p, o);
+    return check_launch();
 }
 
 int blastgpu_dsyrk_potrf_strided(int n, int k, int trans_a, double alpha, const double* A, int lda,

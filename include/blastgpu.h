@@ -90,6 +90,18 @@ int blastgpu_tune_get(const char* key, int* value);
 int blastgpu_selftest_recip(int which, const double* x, double* y, int n, blastgpu_stream_t stream);
 int blastgpu_probe_fp64_tflops(double* tflops, blastgpu_stream_t stream);
 
+/* blastgpu_dposv_strided for operands outside device memory: A and B are read in place and L and
+ * X written in place, each element once, from/to any memory the GPU can address (pinned host
+ * buffers; on hardware-coherent systems such as GB300 any host allocation), so a host-resident batch
+ * is solved in one launch without staging copies. The factorisation re-reads its partial results
+ * from the device workspaces L_work (n*n doubles per instance) and X_work (n*nrhs per instance),
+ * which must be device memory. Same results as blastgpu_dposv_strided, bit for bit.
+ * No reference counterpart (BLAST's matrices are host memory by construction). */
+int blastgpu_dposv_mirror_strided(int n, int nrhs, const double* A, int lda, int64_t stride_a,
+                                  const double* B, int ldb, int64_t stride_b, double* L, int ldl,
+                                  int64_t stride_l, double* X, int ldx, int64_t stride_x, double* L_work,
+                                  double* X_work, int32_t* info, int64_t batch, blastgpu_stream_t stream);
+
 /* D = chol(beta*C + alpha*op(A)*op(A)^T), lower triangle; op(A) = A (n x k) or, with trans_a = 1,
  * the transpose of a k x n A. The Riccati-recursion kernel that BLAST benchmarks as syrk followed
  * by potrf (bench/blas/SyrkPotrf.cpp:15-40; BLASFEO's dsyrk_dpotrf_ln,
