@@ -92,6 +92,23 @@ __global__ void __launch_bounds__(128) trmm_kernel(int side, int m, int n, doubl
 }  // namespace
 }  // namespace blastgpu
 
+namespace blastgpu {
+
+int launch_syrk_lower(int m, int k, int trans_a, double alpha, const double* A, int lda, int64_t sa,
+                      double beta, const double* C, int ldc, int64_t sc, double* D, int ldd, int64_t sd,
+                      int64_t batch, cudaStream_t s) {
+    if (batch == 0 || m == 0) return BLASTGPU_SUCCESS;
+    if ((batch + 3) / 4 > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
+    // op(A) = A^T of a k x m column-major A is the row-major reading of the same storage
+    Strided a{const_cast<double*>(A), lda, sa, trans_a ? BLASTGPU_ROW_MAJOR : BLASTGPU_COL_MAJOR};
+    Strided c{const_cast<double*>(C), ldc, sc, BLASTGPU_COL_MAJOR};
+    Strided d{D, ldd, sd, BLASTGPU_COL_MAJOR};
+    syrk_lower_kernel<<<(unsigned)((batch + 3) / 4), 128, 0, s>>>(m, k, alpha, a, beta, c, d, batch);
+    return check_launch();
+}
+
+}  // namespace blastgpu
+
 using namespace blastgpu;
 
 extern "C" {
@@ -108,13 +125,8 @@ int blastgpu_dsyrk_lower_strided(int m, int k, double alpha, const double* A, in
     if (m > 0 && !D) return -11;
     if (ldd < (m > 0 ? m : 1)) return -12;
     if (batch < 0) return -14;
-    if (batch == 0 || m == 0) return BLASTGPU_SUCCESS;
-    if ((batch + 3) / 4 > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
-    Strided a{const_cast<double*>(A), lda, stride_a, BLASTGPU_COL_MAJOR};
-    Strided c{const_cast<double*>(C), ldc, stride_c, BLASTGPU_COL_MAJOR};
-    Strided d{D, ldd, stride_d, BLASTGPU_COL_MAJOR};
-    syrk_lower_kernel<<<(unsigned)((batch + 3) / 4), 128, 0, as_cuda(stream)>>>(m, k, alpha, a, beta, c, d, batch);
-    return check_launch();
+    return launch_syrk_lower(m, k, 0, alpha, A, lda, stride_a, beta, C, ldc, stride_c, D, ldd, stride_d, batch,
+                             as_cuda(stream));
 }
 
 int blastgpu_dtrsm_strided(int uplo, int trans_a, int unit, int m, int n, const double* A, int lda,

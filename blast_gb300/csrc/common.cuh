@@ -28,6 +28,12 @@ inline cudaStream_t as_cuda(blastgpu_stream_t s) { return reinterpret_cast<cudaS
 // Number of SMs of the current device (cached per device).
 int sm_count();
 
+// D_lower = beta*C + alpha*op(A)*op(A)^T on a uniform batch, syrkLower's order (blas3.cu);
+// op(A) = A (m x k) or, with trans_a, the transpose of a k x m A.
+int launch_syrk_lower(int m, int k, int trans_a, double alpha, const double* A, int lda, int64_t sa,
+                      double beta, const double* C, int ldc, int64_t sc, double* D, int ldd, int64_t sd,
+                      int64_t batch, cudaStream_t s);
+
 // Kernel-selection parameters set by the autotuner (blastgpu_tune_set); `fallback` if unset.
 int tune_get(const char* key, int fallback);
 

@@ -14,6 +14,22 @@ def F(a):
     return np.asfortranarray(a)
 
 
+@pytest.fixture(params=["fused", "two_launch"])
+def path(request, gpu):
+    """Both code paths of blastgpu_dsyrk_potrf_strided: the fused kernel (large batches) and
+    syrkLower then potrf (small batches), forced through the tuning key that separates them."""
+    from blast_gb300 import _lib
+
+    old = _lib.tune_get("syrk_potrf.fused_min_batch")
+    _lib.tune_set("syrk_potrf.fused_min_batch", 0 if request.param == "fused" else 1 << 30)
+    yield request.param
+    if old is None:  # the library's default: 192 instances per SM
+        import torch
+
+        old = torch.cuda.get_device_properties(0).multi_processor_count * 192
+    _lib.tune_set("syrk_potrf.fused_min_batch", old)
+
+
 def _case(rng, batch, n, k):
     A = rng.uniform(-1, 1, (batch, n, k))
     G = rng.uniform(-1, 1, (batch, n, n))
@@ -22,7 +38,7 @@ def _case(rng, batch, n, k):
 
 
 @pytest.mark.parametrize("trans", [False, True])
-def test_syrk_potrf_matches_composition(gpu, oracle_lib, trans):
+def test_syrk_potrf_matches_composition(gpu, oracle_lib, trans, path):
     import torch
 
     rng = np.random.default_rng(31 + trans)
@@ -52,7 +68,7 @@ def test_syrk_potrf_matches_composition(gpu, oracle_lib, trans):
             assert normwise(np.tril(D[b]), np.tril(Lr)) <= 10 * n * EPS, (n, k)
 
 
-def test_syrk_potrf_in_place_and_info(gpu):
+def test_syrk_potrf_in_place_and_info(gpu, path):
     import torch
 
     rng = np.random.default_rng(33)
