@@ -125,6 +125,58 @@ __device__ __forceinline__ int warp_chol32(T (&a)[32], int nb, int lane, T& rdia
     return bad;
 }
 
+// Update of the panel's register tiles with all previous columns: acc -= F(k0:n, kk) * F(k0+c, kk)
+// for kk < k0, the columns streamed through shared memory kKC at a time. RA = row blocks still
+// below the diagonal (ceil(m / 32)), fixed at compile time so that the inner loop is RA x 4
+// fused multiply-adds with no per-row guards. Rows past m and columns past nb pick up stale
+// shared-memory values; they are never stored.
+template <typename T, int RA, int MAXR>
+__device__ __forceinline__ void panel_update(T (&acc)[MAXR][4], const T* F, int ldf, T* buf, int k0, int m,
+                                             int c0) {
+    constexpr int NMAX = 32 * MAXR;
+    int const tid = threadIdx.x, lane = tid & 31;
+    for (int kk = 0; kk < k0; kk += kKC) {
+        int const kc = min(kKC, k0 - kk);
+        __syncthreads();
+        for (int q = 0; q < kc; ++q) {
+            T const* src = F + k0 + (int64_t)(kk + q) * ldf;
+            for (int r = tid; r < m; r += kThreads) cp_async(buf + q * NMAX + r, src + r);
+        }
+        cp_async_wait_all();
+        __syncthreads();
+#pragma unroll 2
+        for (int q = 0; q < kc; ++q) {
+            T const* col = buf + q * NMAX;
+            T b[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) b[j] = col[c0 + j];
+#pragma unroll
+            for (int i = 0; i < RA; ++i) {
+                T const a = col[lane + 32 * i];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fma(-a, b[j], acc[i][j]);
+            }
+        }
+    }
+}
+
+template <typename T, int MAXR>
+__device__ __forceinline__ void panel_update_dispatch(T (&acc)[MAXR][4], const T* F, int ldf, T* buf, int k0,
+                                                      int m, int c0) {
+    switch ((m + 31) / 32) {
+#define BLASTGPU_PANEL_CASE(R) \
+    case R:                    \
+        if constexpr (R <= MAXR) panel_update<T, R, MAXR>(acc, F, ldf, buf, k0, m, c0); \
+        break;
+        BLASTGPU_PANEL_CASE(1) BLASTGPU_PANEL_CASE(2) BLASTGPU_PANEL_CASE(3) BLASTGPU_PANEL_CASE(4)
+        BLASTGPU_PANEL_CASE(5) BLASTGPU_PANEL_CASE(6) BLASTGPU_PANEL_CASE(7) BLASTGPU_PANEL_CASE(8)
+        BLASTGPU_PANEL_CASE(9) BLASTGPU_PANEL_CASE(10) BLASTGPU_PANEL_CASE(11) BLASTGPU_PANEL_CASE(12)
+        BLASTGPU_PANEL_CASE(13) BLASTGPU_PANEL_CASE(14) BLASTGPU_PANEL_CASE(15) BLASTGPU_PANEL_CASE(16)
+#undef BLASTGPU_PANEL_CASE
+        default: break;
+    }
+}
+
 // Left-looking blocked Cholesky of the n x n matrix: lower(A) -> F (precision T, ld ldf).
 // Returns info (0 or first bad pivot + 1) identically in all threads.
 template <typename T, int MAXR>
@@ -147,32 +199,8 @@ __device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf,
                 acc[i][j] = (r < m && c < nb && r >= c) ? (T)A[(k0 + r) + (int64_t)(k0 + c) * lda] : (T)0;
             }
         }
-        // Panel update with the previous columns: acc -= F(k0:n, kk) * F(k0+c, kk)
-        for (int kk = 0; kk < k0; kk += kKC) {
-            int const kc = min(kKC, k0 - kk);
-            __syncthreads();
-            for (int q = 0; q < kc; ++q) {
-                T const* src = F + k0 + (int64_t)(kk + q) * ldf;
-                for (int r = tid; r < m; r += kThreads) cp_async(buf + q * NMAX + r, src + r);
-            }
-            cp_async_wait_all();
-            __syncthreads();
-            for (int q = 0; q < kc; ++q) {
-                T const* col = buf + q * NMAX;
-                T b[4];
-#pragma unroll
-                for (int j = 0; j < 4; ++j) b[j] = (c0 + j < nb) ? col[c0 + j] : (T)0;
-#pragma unroll
-                for (int i = 0; i < MAXR; ++i) {
-                    int const r = lane + 32 * i;
-                    if (i * 32 < m) {
-                        T const a = r < m ? col[r] : (T)0;
-#pragma unroll
-                        for (int j = 0; j < 4; ++j) acc[i][j] = fma(-a, b[j], acc[i][j]);
-                    }
-                }
-            }
-        }
+        // Panel update with the previous columns.
+        panel_update_dispatch<T, MAXR>(acc, F, ldf, buf, k0, m, c0);
         __syncthreads();
         // Panel to shared memory, column-major with stride NMAX.
 #pragma unroll
