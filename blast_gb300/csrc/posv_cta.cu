@@ -100,31 +100,6 @@ struct Smem {
         sizeof(T) * (kBufElems + kBlkElems) + sizeof(double) * (4 * NMAX + 64);
 };
 
-// Cholesky of the nb x nb diagonal block held in registers, lane = row (a[k] = block(lane, k)),
-// fully unrolled: step j takes the pivot from lane j, scales column j, and updates the trailing
-// lower part with column j fetched from the owning lanes by shuffles. rdiag receives 1/l_jj on
-// lane j. Returns (on every lane) the first bad pivot + 1 within the block, or 0.
-template <typename T>
-__device__ __forceinline__ int warp_chol32(T (&a)[32], int nb, int lane, T& rdiag) {
-    int bad = 0;
-#pragma unroll
-    for (int j = 0; j < 32; ++j) {
-        if (j < nb) {
-            T const d = __shfl_sync(0xffffffffu, a[j], j);
-            if (!(d > (T)0) && bad == 0) bad = j + 1;
-            T const y = rsqrt_t<T>(d);
-            if (lane == j) { rdiag = y; a[j] = d * y; }
-            else if (lane > j) a[j] *= y;
-#pragma unroll
-            for (int l = j + 1; l < 32; ++l) {
-                T const llj = __shfl_sync(0xffffffffu, a[j], l);
-                if (lane >= l && l < nb) a[l] = fma(-a[j], llj, a[l]);
-            }
-        }
-    }
-    return bad;
-}
-
 // Update of the panel's register tiles with all previous columns: acc -= F(k0:n, kk) * F(k0+c, kk)
 // for kk < k0, the columns streamed through shared memory kKC at a time. RA = row blocks still
 // below the diagonal (ceil(m / 32)), fixed at compile time so that the inner loop is RA x 4
@@ -177,10 +152,47 @@ __device__ __forceinline__ void panel_update_dispatch(T (&acc)[MAXR][4], const T
     }
 }
 
+// Cholesky of the nb x nb diagonal block held in shared memory (column j at blk + j * NMAX),
+// right-looking, all threads: step j takes the pivot d = a_jj, y = 1/sqrt(d), and updates the
+// trailing block a_il = fma(-(a_ij*y), (a_lj*y), a_il) (warp w: columns l = j+1+w, j+1+w+8, ...;
+// lane: row l + lane); column j itself is scaled during step j+1, when nobody reads it any more.
+// One barrier per step. rinv[j] = y. Records the first bad pivot (k0 + j + 1) in *s_info.
+template <typename T, int NMAX>
+__device__ __forceinline__ void cta_chol_block(T* blk, int nb, int k0, T* rinv, int* s_info) {
+    int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    T dprev = (T)1, yprev = (T)1;
+    for (int j = 0; j < nb; ++j) {
+        T const d = blk[j * NMAX + j];
+        T const y = rsqrt_t<T>(d);
+        if (tid == 0) {
+            if (!(d > (T)0) && *s_info == 0) *s_info = k0 + j + 1;
+            rinv[j] = y;
+        }
+        if (j > 0 && tid < nb - (j - 1)) {
+            int const i = j - 1 + tid;
+            T* c = blk + (j - 1) * NMAX;
+            c[i] = i == j - 1 ? dprev * yprev : c[i] * yprev;
+        }
+        T const* cj = blk + j * NMAX;
+        for (int l = j + 1 + warp; l < nb; l += kWarps) {
+            int const i = l + lane;
+            if (i < nb) blk[l * NMAX + i] = fma(-(cj[i] * y), cj[l] * y, blk[l * NMAX + i]);
+        }
+        dprev = d;
+        yprev = y;
+        __syncthreads();
+    }
+    if (nb > 0 && tid < 1) blk[(nb - 1) * NMAX + (nb - 1)] = dprev * yprev;
+    __syncthreads();
+}
+
 // Left-looking blocked Cholesky of the n x n matrix: lower(A) -> F (precision T, ld ldf).
-// Returns info (0 or first bad pivot + 1) identically in all threads.
+// Returns info (0 or first bad pivot + 1) identically in all threads. With rowsum (n doubles in
+// shared memory, zeroed by the caller), also accumulates the row sums of |A| of the symmetric
+// matrix from the lower triangle it reads (|A|_inf = max rowsum), so that A is read once.
 template <typename T, int MAXR>
-__device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf, int* s_info) {
+__device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf, int* s_info,
+                         double* rowsum = nullptr) {
     constexpr int NMAX = 32 * MAXR;
     __shared__ T rinv[kNB];
     int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -190,13 +202,30 @@ __device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf,
         int const m = n - k0;
         int const c0 = warp * 4;  // this warp's panel columns c0..c0+3 (relative to k0)
         T acc[MAXR][4];
+        double csum[4] = {0.0, 0.0, 0.0, 0.0};  // |a| below the diagonal, per panel column
 #pragma unroll
         for (int i = 0; i < MAXR; ++i) {
             int const r = lane + 32 * i;  // row relative to k0
+            double rs = 0.0;
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 int const c = c0 + j;
-                acc[i][j] = (r < m && c < nb && r >= c) ? (T)A[(k0 + r) + (int64_t)(k0 + c) * lda] : (T)0;
+                double const v = (r < m && c < nb && r >= c) ? A[(k0 + r) + (int64_t)(k0 + c) * lda] : 0.0;
+                acc[i][j] = (T)v;
+                if (rowsum) {
+                    rs += fabs(v);
+                    if (r > c) csum[j] += fabs(v);
+                }
+            }
+            if (rowsum && r < m && rs != 0.0) atomicAdd(rowsum + k0 + r, rs);
+        }
+        if (rowsum) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                double v = csum[j];
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+                if (lane == 0 && c0 + j < nb) atomicAdd(rowsum + k0 + c0 + j, v);
             }
         }
         // Panel update with the previous columns.
@@ -213,22 +242,8 @@ __device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf,
             }
         }
         __syncthreads();
-        // Diagonal block (nb x nb): one warp, in registers (lane = row).
-        if (warp == 0) {
-            T a[32];
-#pragma unroll
-            for (int k = 0; k < 32; ++k) a[k] = (k < nb && lane < nb) ? buf[k * NMAX + lane] : (T)0;
-            T rd = (T)0;
-            int const bad = warp_chol32<T>(a, nb, lane, rd);
-            if (bad && lane == 0 && *s_info == 0) *s_info = k0 + bad;
-            if (lane < nb) {
-#pragma unroll
-                for (int k = 0; k < 32; ++k)
-                    if (k <= lane) buf[k * NMAX + lane] = a[k];
-                rinv[lane] = rd;
-            }
-        }
-        __syncthreads();
+        // Diagonal block (nb x nb), all threads, in shared memory.
+        cta_chol_block<T, NMAX>(buf, nb, k0, rinv, s_info);
         // Rows below the block: x_j = (p_j - sum_{q<j} x_q l_jq) / l_jj, one thread per row, the
         // row in registers and the block's entries broadcast from shared memory.
         for (int r = nb + tid; r < m; r += kThreads) {
@@ -473,54 +488,15 @@ __global__ void __launch_bounds__(kThreads, 2) posv_cta_mixed_kernel(Batch batch
     CtaItem const it = batch.get(b);
     int const n = it.n, tid = threadIdx.x;
     float* F = reinterpret_cast<float*>(it.ws);
-    int const info = cta_potrf<float, MAXR>(n, it.A, it.lda, F, n, buf, &s_info);
+    for (int i = tid; i < n; i += kThreads) r[i] = 0.0;
+    __syncthreads();
+    // the factorisation also leaves the row sums of |A| in r
+    int const info = cta_potrf<float, MAXR>(n, it.A, it.lda, F, n, buf, &s_info, r);
     if (tid == 0 && args.info) args.info[b] = info;
 
-    // |A|_inf from the lower triangle: row sums of |A(i,j)| over j<=i plus column sums below.
+    // |A|_inf = max row sum of |A| (accumulated by the factorisation from the lower triangle)
     double anorm;
     {
-        for (int p = tid; p < (n + 1) / 2; p += kThreads) {
-            int const q = n - 1 - p;
-            double s0[4] = {0.0, 0.0, 0.0, 0.0}, s1[4] = {0.0, 0.0, 0.0, 0.0};
-            int j = 0;
-            for (; j + 3 <= p; j += 4) {
-                double ap[4], aq[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    ap[u] = it.A[p + (int64_t)(j + u) * it.lda];
-                    aq[u] = it.A[q + (int64_t)(j + u) * it.lda];
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    s0[u] += fabs(ap[u]);
-                    s1[u] += fabs(aq[u]);
-                }
-            }
-            for (; j <= p; ++j) {
-                s0[0] += fabs(it.A[p + (int64_t)j * it.lda]);
-                s1[0] += fabs(it.A[q + (int64_t)j * it.lda]);
-            }
-            for (; j + 3 <= q; j += 4) {
-                double aq[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) aq[u] = it.A[q + (int64_t)(j + u) * it.lda];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) s1[u] += fabs(aq[u]);
-            }
-            for (; j <= q; ++j) s1[0] += fabs(it.A[q + (int64_t)j * it.lda]);
-            r[p] = (s0[0] + s0[1]) + (s0[2] + s0[3]);
-            if (q != p) r[q] = (s1[0] + s1[1]) + (s1[2] + s1[3]);
-        }
-        __syncthreads();
-        int const lane = tid & 31, warp = tid >> 5;
-        for (int i = warp; i < n; i += kWarps) {
-            double s = 0.0;
-            for (int j = i + 1 + lane; j < n; j += 32) s += fabs(it.A[j + (int64_t)i * it.lda]);
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-            if (lane == 0) r[i] += s;
-        }
-        __syncthreads();
         double m = 0.0;
         for (int i = tid; i < n; i += kThreads) m = fmax(m, r[i]);
         anorm = cta_max(m, red);
