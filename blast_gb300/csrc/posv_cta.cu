@@ -189,7 +189,9 @@ __device__ __forceinline__ void cta_chol_block(T* blk, int nb, int k0, T* rinv, 
 // Left-looking blocked Cholesky of the n x n matrix: lower(A) -> F (precision T, ld ldf).
 // Returns info (0 or first bad pivot + 1) identically in all threads. With rowsum (n doubles in
 // shared memory, zeroed by the caller), also accumulates the row sums of |A| of the symmetric
-// matrix from the lower triangle it reads (|A|_inf = max rowsum), so that A is read once.
+// matrix from the lower triangle it reads (|A|_inf = max rowsum), so that A is read once: per
+// panel, every warp leaves its rows' partial sums (and its columns' sums below the diagonal) in
+// the staging buffer, and one thread per row adds them up.
 template <typename T, int MAXR>
 __device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf, int* s_info,
                          double* rowsum = nullptr) {
@@ -202,30 +204,39 @@ __device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf,
         int const m = n - k0;
         int const c0 = warp * 4;  // this warp's panel columns c0..c0+3 (relative to k0)
         T acc[MAXR][4];
-        double csum[4] = {0.0, 0.0, 0.0, 0.0};  // |a| below the diagonal, per panel column
+        float csum[4] = {0.f, 0.f, 0.f, 0.f};  // |a| below the diagonal, per panel column
 #pragma unroll
         for (int i = 0; i < MAXR; ++i) {
             int const r = lane + 32 * i;  // row relative to k0
-            double rs = 0.0;
+            float rs = 0.f;  // binary32 sums: |A|_inf only scales the backward error
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 int const c = c0 + j;
                 double const v = (r < m && c < nb && r >= c) ? A[(k0 + r) + (int64_t)(k0 + c) * lda] : 0.0;
                 acc[i][j] = (T)v;
                 if (rowsum) {
-                    rs += fabs(v);
-                    if (r > c) csum[j] += fabs(v);
+                    float const av = fabsf((float)v);
+                    rs += av;
+                    if (r > c) csum[j] += av;
                 }
             }
-            if (rowsum && r < m && rs != 0.0) atomicAdd(rowsum + k0 + r, rs);
+            if (rowsum && r < m) reinterpret_cast<double*>(buf)[warp * NMAX + r] = rs;
         }
         if (rowsum) {
+            double* part = reinterpret_cast<double*>(buf);  // [kWarps][NMAX] rows, then [kNB] columns
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                double v = csum[j];
+                float v = csum[j];
 #pragma unroll
                 for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-                if (lane == 0 && c0 + j < nb) atomicAdd(rowsum + k0 + c0 + j, v);
+                if (lane == 0) part[kWarps * NMAX + c0 + j] = v;
+            }
+            __syncthreads();
+            for (int r = tid; r < m; r += kThreads) {
+                double t = r < nb ? part[kWarps * NMAX + r] : 0.0;
+#pragma unroll
+                for (int w = 0; w < kWarps; ++w) t += part[w * NMAX + r];
+                rowsum[k0 + r] += t;
             }
         }
         // Panel update with the previous columns.
@@ -397,6 +408,19 @@ __device__ void cta_symv_lower(int n, const double* A, int lda, const double* x,
         int const q = n - 1 - p;
         double a0[4] = {0.0, 0.0, 0.0, 0.0}, a1[4] = {0.0, 0.0, 0.0, 0.0};
         int j = 0;
+        for (; j + 7 <= p; j += 8) {  // 16 loads in flight per thread
+            double ap[8], aq[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                ap[u] = A[p + (int64_t)(j + u) * lda];
+                aq[u] = A[q + (int64_t)(j + u) * lda];
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                a0[u & 3] = fma(ap[u], x[j + u], a0[u & 3]);
+                a1[u & 3] = fma(aq[u], x[j + u], a1[u & 3]);
+            }
+        }
         for (; j + 3 <= p; j += 4) {
             double ap[4], aq[4];
 #pragma unroll
@@ -414,6 +438,13 @@ __device__ void cta_symv_lower(int n, const double* A, int lda, const double* x,
             a0[0] = fma(A[p + (int64_t)j * lda], x[j], a0[0]);
             a1[0] = fma(A[q + (int64_t)j * lda], x[j], a1[0]);
         }
+        for (; j + 15 <= q; j += 16) {  // the long row alone: 16 loads in flight
+            double aq[16];
+#pragma unroll
+            for (int u = 0; u < 16; ++u) aq[u] = A[q + (int64_t)(j + u) * lda];
+#pragma unroll
+            for (int u = 0; u < 16; ++u) a1[u & 3] = fma(aq[u], x[j + u], a1[u & 3]);
+        }
         for (; j + 3 <= q; j += 4) {
             double aq[4];
 #pragma unroll
@@ -426,12 +457,36 @@ __device__ void cta_symv_lower(int n, const double* A, int lda, const double* x,
         if (q != p) y[q] = (a1[0] + a1[1]) + (a1[2] + a1[3]);
     }
     __syncthreads();
-    for (int i = warp; i < n; i += kWarps) {
-        double acc = 0.0;
-        for (int j = i + 1 + lane; j < n; j += 32) acc = fma(A[j + (int64_t)i * lda], x[j], acc);
+    // strictly lower columns: a warp takes four columns at a time (i, i+8, i+16, i+24), lanes over
+    // rows, two 32-row chunks of each column in flight
+    for (int i0 = warp; i0 < n; i0 += 4 * kWarps) {
+        double acc[4][2] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
+        int const base = i0 + 1 + lane;  // first row below column i0 for this lane
+        for (int j = base; j < n; j += 64) {
+            double a[4][2];
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-        if (lane == 0) y[i] += acc;
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    int const i = i0 + kWarps * u, jj = j + 32 * h;
+                    a[u][h] = (i < n && jj > i && jj < n) ? A[jj + (int64_t)i * lda] : 0.0;
+                }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    int const jj = j + 32 * h;
+                    acc[u][h] = fma(a[u][h], jj < n ? x[jj] : 0.0, acc[u][h]);
+                }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            int const i = i0 + kWarps * u;
+            double s = acc[u][0] + acc[u][1];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+            if (lane == 0 && i < n) y[i] += s;
+        }
     }
     __syncthreads();
 }
