@@ -632,8 +632,10 @@ struct DescBwd {
 };
 
 template <int MAXR, class Batch>
-__global__ void __launch_bounds__(kThreads, 1) posv_bwd_kernel(Batch batch, int64_t count, int recompute,
-                                                               int32_t* info) {
+// Two CTAs per SM up to n = 128 (MAXR <= 4 fits 128 registers per thread); larger bins keep the
+// register budget of one CTA per SM.
+__global__ void __launch_bounds__(kThreads, MAXR <= 4 ? 2 : 1)
+    posv_bwd_kernel(Batch batch, int64_t count, int recompute, int32_t* info) {
     using S = Smem<double, MAXR>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double* buf = reinterpret_cast<double*>(smem_raw);
@@ -658,15 +660,29 @@ __global__ void __launch_bounds__(kThreads, 1) posv_bwd_kernel(Batch batch, int6
         for (int i = tid; i < n; i += kThreads) it.GB[i + (int64_t)c * it.ldgb] = vec[i];
         __syncthreads();
     }
-    for (int e = tid; e < n * n; e += kThreads) {
-        int const i = e % n, j = e / n;
-        double acc = 0.0;
-        for (int c = 0; c < it.nrhs; ++c) {
-            acc = fma(it.GB[i + (int64_t)c * it.ldgb], it.X[j + (int64_t)c * it.ldx], acc);
-            acc = fma(it.X[i + (int64_t)c * it.ldx], it.GB[j + (int64_t)c * it.ldgb], acc);
+    // GA = -sym(GB X^T): warp per column, lanes over rows (coalesced stores). With one
+    // right-hand side, GB (still in vec) and X come from shared memory.
+    int const lane = tid & 31, warp = tid >> 5;
+    if (it.nrhs == 1) {
+        double* xs = vec + S::NMAX;
+        for (int i = tid; i < n; i += kThreads) xs[i] = it.X[i];
+        __syncthreads();
+        for (int j = warp; j < n; j += kWarps) {
+            double const xj = xs[j], gj = vec[j];
+            double* ga = it.GA + (int64_t)j * it.ldga;
+            for (int i = lane; i < n; i += 32) ga[i] = -0.5 * fma(xs[i], gj, vec[i] * xj);
         }
-        it.GA[i + (int64_t)j * it.ldga] = -0.5 * acc;
+        return;
     }
+    for (int j = warp; j < n; j += kWarps)
+        for (int i = lane; i < n; i += 32) {
+            double acc = 0.0;
+            for (int c = 0; c < it.nrhs; ++c) {
+                acc = fma(it.GB[i + (int64_t)c * it.ldgb], it.X[j + (int64_t)c * it.ldx], acc);
+                acc = fma(it.X[i + (int64_t)c * it.ldx], it.GB[j + (int64_t)c * it.ldgb], acc);
+            }
+            it.GA[i + (int64_t)j * it.ldga] = -0.5 * acc;
+        }
 }
 
 // Raises a kernel's dynamic shared-memory limit once per process (before any stream capture
