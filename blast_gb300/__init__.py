@@ -6,10 +6,10 @@ torch device tensors.
 """
 from . import _lib
 from .blast import (LEFT, LOWER, RIGHT, UPPER, col_major, gemm, ger, getrf, getrs, iamax, laswp,
-                    posv, potrf, potrs, swap, syrk_lower, syrk_potrf, trmm, trsm, trsv_left_lower,
+                    posv, potrf, potrs, swap, syrk_lower, syrk_potrf, trmm, trsm, trsm_right, trsv_left_lower,
                     trsv_left_upper)
 
-__all__ = ["gemm", "potrf", "posv", "potrs", "getrf", "getrs", "syrk_lower", "syrk_potrf", "trsm", "trmm", "ger",
+__all__ = ["gemm", "potrf", "posv", "potrs", "getrf", "getrs", "syrk_lower", "syrk_potrf", "trsm", "trsm_right", "trmm", "ger",
            "iamax", "laswp", "swap", "trsv_left_lower", "trsv_left_upper", "col_major", "LOWER",
            "UPPER", "LEFT", "RIGHT", "_lib"]
 

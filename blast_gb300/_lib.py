@@ -65,6 +65,8 @@ SIGNATURES: dict[str, list] = {
                                       PTR, PTR, PTR, I64, PTR],
     "blastgpu_dsyrk_potrf_strided": [I32, I32, I32, DBL, PTR, I32, I64, DBL, PTR, I32, I64, PTR, I32, I64, PTR,
                                      I64, PTR],
+    "blastgpu_dtrsm_right_strided": [I32, I32, I32, I32, I32, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, I64,
+                                     PTR],
     "blastgpu_dger_strided": [I32, I32, DBL, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, I64, PTR],
     "blastgpu_idamax_strided": [I32, PTR, I32, I64, PTR, I64, PTR],
     "blastgpu_dlaswp_strided": [I32, PTR, I32, I64, I32, I32, PTR, I64, I64, PTR],

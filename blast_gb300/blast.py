@@ -273,8 +273,8 @@ def trsm(uplo: int, unit: bool, A: torch.Tensor, B: torch.Tensor, X: torch.Tenso
 def trmm(alpha, *args) -> torch.Tensor:
     """C = alpha*A*B: trmm(alpha, A, uplo, diag, B, C)  (algorithm/Trmm.hpp:260-283), or
     C = alpha*B*A: trmm(alpha, B, A, uplo, diag, C)  (algorithm/Trmm.hpp:287-310).
-    BLAST implements A upper for the left product and A lower for the right one, non-unit only;
-    the other variants raise NotImplementedError (BLAST: std::logic_error)."""
+    BLAST implements A upper for the left product and A lower for the right one, non-unit only
+    (std::logic_error otherwise); all (side, uplo, diag) combinations are computed here."""
     if len(args) != 5:
         raise TypeError("trmm(alpha, A, uplo, diag, B, C) or trmm(alpha, B, A, uplo, diag, C)")
     if isinstance(args[1], torch.Tensor):
@@ -294,11 +294,26 @@ def trmm(alpha, *args) -> torch.Tensor:
     st = _lib.lib().blastgpu_dtrmm_strided(side, int(uplo), int(bool(diag)), m, n, float(alpha), a.ptr,
                                            a.ld, _bstride(a, batch), b.ptr, b.ld, _bstride(b, batch),
                                            c.ptr, c.ld, c.bstride, batch, _stream())
-    if st == -1001:
-        raise NotImplementedError("trmm variant not implemented (BLAST throws std::logic_error)")
     if st != 0:
         raise _lib.BlastGpuError("blastgpu_dtrmm_strided", st)
     return C
+
+
+def trsm_right(uplo: int, unit: bool, A: torch.Tensor, B: torch.Tensor, X: torch.Tensor) -> torch.Tensor:
+    """Solve X*A = B, A triangular (no BLAST counterpart: RegisterMatrix::trsm leaves the right side
+    unimplemented, register_matrix/RegisterMatrix.hpp:592-597). A may be a row-major tensor
+    (transposed view); X may be B."""
+    a, b, x = _as_mat(A, "A"), _as_mat(B, "B"), _as_mat(X, "X")
+    m, n = b.rows, b.cols
+    if a.rows != n or a.cols != n or x.rows != m or x.cols != n:
+        raise ValueError("Invalid argument size")
+    _square_col(b, "B")
+    _square_col(x, "X")
+    batch = _batch_of(a, b, x)
+    _lib.call("blastgpu_dtrsm_right_strided", int(uplo), int(a.layout == ROW), int(bool(unit)), m, n, a.ptr,
+              a.ld, _bstride(a, batch), b.ptr, b.ld, _bstride(b, batch), x.ptr, x.ld, x.bstride, batch,
+              _stream())
+    return X
 
 
 def _vec(v: torch.Tensor, name: str):

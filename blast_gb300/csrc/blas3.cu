@@ -9,9 +9,13 @@
 //    transposed view (the potrs backward solve uses trsm<Upper> on trans(L)).
 //  * blast::trmm (algorithm/Trmm.hpp:93-242, RegisterMatrix::trmm :745-880):
 //    left upper  c_ij = sum_{k>=i} fma(alpha*a_ik, b_kj, .), k ascending from 0-accumulator;
-//    right lower c_ij = sum_{k>=j} fma(alpha*b_ik, a_kj, .). Other (side, uplo) pairs and unit
-//    diagonals are not implemented by BLAST (std::logic_error) and return
-//    BLASTGPU_ERR_NOT_IMPLEMENTED here.
+//    right lower c_ij = sum_{k>=j} fma(alpha*b_ik, a_kj, .).
+//    BLAST throws std::logic_error for the other (side, uplo) pairs and for unit diagonals
+//    (algorithm/Trmm.hpp:101-124, 240); they are computed here in the same pattern: left lower
+//    over k = 0..i, right upper over k = 0..j, k ascending, a unit diagonal read as 1.
+//  * Right-side triangular solve X op(A) = B (RegisterMatrix.hpp:592-597 leaves it unimplemented;
+//    no BLAST counterpart): per row i, op(A) upper: j ascending, acc = b_ij, for k < j ascending
+//    acc = fma(-x_ik, a_kj, acc); lower: j descending, k > j ascending; non-unit x_ij = acc / a_jj.
 //
 // GPU mapping: syrk and trmm run one warp per instance with lanes over output elements (every
 // element is an independent chain of fused multiply-adds); trsm runs one thread per
@@ -72,20 +76,47 @@ __global__ void __launch_bounds__(128) trsm_kernel(int uplo, int trans_a, int un
     }
 }
 
-__global__ void __launch_bounds__(128) trmm_kernel(int side, int m, int n, double alpha, Strided A, Strided B,
-                                                   Strided C, int64_t batch) {
+__global__ void __launch_bounds__(128) trmm_kernel(int side, int uplo, int unit, int m, int n, double alpha,
+                                                   Strided A, Strided B, Strided C, int64_t batch) {
     int64_t const b = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5);
     int const lane = threadIdx.x & 31;
     if (b >= batch) return;
+    auto a = [&](int i, int q) -> double { return (unit && i == q) ? 1.0 : A.at(b, i, q); };
+    bool const upper = uplo == BLASTGPU_UPPER;
     for (int e = lane; e < m * n; e += 32) {
         int const i = e % m, j = e / m;
         double acc = 0.0;
         if (side == BLASTGPU_LEFT) {
-            for (int q = i; q < m; ++q) acc = fma(alpha * A.at(b, i, q), B.at(b, q, j), acc);
+            int const q0 = upper ? i : 0, q1 = upper ? m : i + 1;
+            for (int q = q0; q < q1; ++q) acc = fma(alpha * a(i, q), B.at(b, q, j), acc);
         } else {
-            for (int q = j; q < n; ++q) acc = fma(alpha * B.at(b, i, q), A.at(b, q, j), acc);
+            int const q0 = upper ? 0 : j, q1 = upper ? j + 1 : n;
+            for (int q = q0; q < q1; ++q) acc = fma(alpha * B.at(b, i, q), a(q, j), acc);
         }
         C.at(b, i, j) = acc;
+    }
+}
+
+// X op(A) = B, one thread per (instance, row of X).
+__global__ void __launch_bounds__(128) trsm_right_kernel(int uplo, int trans_a, int unit, int m, int n, Strided A,
+                                                         Strided B, Strided X, int64_t batch) {
+    int64_t const t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= batch * m) return;
+    int64_t const b = t / m;
+    int const i = (int)(t - b * m);
+    auto a = [&](int q, int j) -> double { return trans_a ? A.at(b, j, q) : A.at(b, q, j); };
+    if (uplo == BLASTGPU_UPPER) {
+        for (int j = 0; j < n; ++j) {
+            double acc = B.at(b, i, j);
+            for (int q = 0; q < j; ++q) acc = fma(-X.at(b, i, q), a(q, j), acc);
+            X.at(b, i, j) = unit ? acc : acc / a(j, j);
+        }
+    } else {
+        for (int j = n; j-- > 0;) {
+            double acc = B.at(b, i, j);
+            for (int q = j + 1; q < n; ++q) acc = fma(-X.at(b, i, q), a(q, j), acc);
+            X.at(b, i, j) = unit ? acc : acc / a(j, j);
+        }
     }
 }
 
@@ -170,17 +201,39 @@ int blastgpu_dtrmm_strided(int side, int uplo, int unit, int m, int n, double al
     if (m > 0 && n > 0 && !C) return -13;
     if (ldc < (m > 0 ? m : 1)) return -14;
     if (batch < 0) return -16;
-    // BLAST implements left-upper and right-lower with a non-unit diagonal only
-    // (algorithm/Trmm.hpp:101-102, 124, 240).
-    if (unit) return BLASTGPU_ERR_NOT_IMPLEMENTED;
-    if (side == BLASTGPU_LEFT && uplo != BLASTGPU_UPPER) return BLASTGPU_ERR_NOT_IMPLEMENTED;
-    if (side == BLASTGPU_RIGHT && uplo != BLASTGPU_LOWER) return BLASTGPU_ERR_NOT_IMPLEMENTED;
     if (batch == 0 || m == 0 || n == 0) return BLASTGPU_SUCCESS;
     if ((batch + 3) / 4 > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
     Strided a{const_cast<double*>(A), lda, stride_a, BLASTGPU_COL_MAJOR};
     Strided bb{const_cast<double*>(B), ldb, stride_b, BLASTGPU_COL_MAJOR};
     Strided c{C, ldc, stride_c, BLASTGPU_COL_MAJOR};
-    trmm_kernel<<<(unsigned)((batch + 3) / 4), 128, 0, as_cuda(stream)>>>(side, m, n, alpha, a, bb, c, batch);
+    trmm_kernel<<<(unsigned)((batch + 3) / 4), 128, 0, as_cuda(stream)>>>(side, uplo, unit, m, n, alpha, a, bb, c,
+                                                                         batch);
+    return check_launch();
+}
+
+int blastgpu_dtrsm_right_strided(int uplo, int trans_a, int unit, int m, int n, const double* A, int lda,
+                                 int64_t stride_a, const double* B, int ldb, int64_t stride_b, double* X,
+                                 int ldx, int64_t stride_x, int64_t batch, blastgpu_stream_t stream) {
+    if (uplo != BLASTGPU_LOWER && uplo != BLASTGPU_UPPER) return -1;
+    if (trans_a != 0 && trans_a != 1) return -2;
+    if (unit != 0 && unit != 1) return -3;
+    if (m < 0) return -4;
+    if (n < 0) return -5;
+    if (n > 0 && !A) return -6;
+    if (lda < (n > 0 ? n : 1)) return -7;
+    if (m > 0 && n > 0 && !B) return -9;
+    if (ldb < (m > 0 ? m : 1)) return -10;
+    if (m > 0 && n > 0 && !X) return -12;
+    if (ldx < (m > 0 ? m : 1)) return -13;
+    if (batch < 0) return -15;
+    if (batch == 0 || m == 0 || n == 0) return BLASTGPU_SUCCESS;
+    int64_t const threads = batch * m;
+    if ((threads + 127) / 128 > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
+    Strided a{const_cast<double*>(A), lda, stride_a, BLASTGPU_COL_MAJOR};
+    Strided bb{const_cast<double*>(B), ldb, stride_b, BLASTGPU_COL_MAJOR};
+    Strided x{X, ldx, stride_x, BLASTGPU_COL_MAJOR};
+    trsm_right_kernel<<<(unsigned)((threads + 127) / 128), 128, 0, as_cuda(stream)>>>(uplo, trans_a, unit, m, n, a,
+                                                                                    bb, x, batch);
     return check_launch();
 }
 

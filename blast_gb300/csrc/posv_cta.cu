@@ -502,7 +502,7 @@ struct CtaArgs {
 
 // Plain binary64 path: factor into L, then X = A^{-1} B column by column.
 template <int MAXR, class Batch>
-__global__ void __launch_bounds__(kThreads, MAXR <= 4 ? 2 : 1) posv_cta_f64_kernel(Batch batch, CtaArgs args) {
+__global__ void __launch_bounds__(kThreads, MAXR <= 8 ? 2 : 1) posv_cta_f64_kernel(Batch batch, CtaArgs args) {
     using S = Smem<double, MAXR>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double* buf = reinterpret_cast<double*>(smem_raw);

@@ -192,12 +192,20 @@ int blastgpu_dtrsm_strided(int uplo, int trans_a, int unit, int m, int n, const 
                            int64_t stride_a, const double* B, int ldb, int64_t stride_b, double* X,
                            int ldx, int64_t stride_x, int64_t batch, blastgpu_stream_t stream);
 
-/* trmm: C = alpha*A*B (side = LEFT, A m x m upper) or C = alpha*B*A (side = RIGHT, A n x n lower),
- * B and C m x n column-major; C must not overlap A or B. Replaces blast::trmm(alpha, A, uplo, diag,
- * B, C) and blast::trmm(alpha, B, A, uplo, diag, C) (algorithm/Trmm.hpp:260-310). As in BLAST, the
- * other (side, uplo) pairs and unit diagonals are not implemented: BLASTGPU_ERR_NOT_IMPLEMENTED
- * (BLAST throws std::logic_error, algorithm/Trmm.hpp:101-124, 240). Only the named triangle of A
- * is read. */
+/* trmm: C = alpha*A*B (side = LEFT, A m x m) or C = alpha*B*A (side = RIGHT, A n x n), A triangular
+ * (uplo; unit = 1: unit diagonal, not read), B and C m x n column-major; C must not overlap A or B.
+ * Replaces blast::trmm(alpha, A, uplo, diag, B, C) and blast::trmm(alpha, B, A, uplo, diag, C)
+ * (algorithm/Trmm.hpp:260-310), bit-identical for the variants BLAST implements (left upper, right
+ * lower, non-unit). BLAST throws std::logic_error for the others (algorithm/Trmm.hpp:101-124, 240);
+ * they are computed here in the same per-element pattern. Only the named triangle of A is read. */
+/* Right-side solve X*op(A) = B for X, A n x n triangular (uplo of op(A)), B and X m x n; X may
+ * equal B. No BLAST counterpart: RegisterMatrix::trsm leaves this side unimplemented
+ * (register_matrix/RegisterMatrix.hpp:592-597). Per row, column substitution with fused
+ * multiply-adds in ascending k and IEEE division by the diagonal. */
+int blastgpu_dtrsm_right_strided(int uplo, int trans_a, int unit, int m, int n, const double* A, int lda,
+                                 int64_t stride_a, const double* B, int ldb, int64_t stride_b, double* X,
+                                 int ldx, int64_t stride_x, int64_t batch, blastgpu_stream_t stream);
+
 int blastgpu_dtrmm_strided(int side, int uplo, int unit, int m, int n, double alpha, const double* A,
                            int lda, int64_t stride_a, const double* B, int ldb, int64_t stride_b,
                            double* C, int ldc, int64_t stride_c, int64_t batch, blastgpu_stream_t stream);

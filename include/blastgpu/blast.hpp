@@ -138,9 +138,13 @@ inline void syrkLower(double alpha, Batch const& A, double beta, Batch const& C,
                   "syrkLower");
 }
 
-// C = alpha*A*B, A triangular (algorithm/Trmm.hpp:260-283)
+// C = alpha*A*B, A triangular (algorithm/Trmm.hpp:260-283). Keeps BLAST's behaviour: the
+// variants BLAST does not implement throw std::logic_error (the C ABI computes them).
 inline void trmm(double alpha, Batch const& A, UpLo uplo, bool diag, Batch const& B, Batch const& C,
                  blastgpu_stream_t stream = nullptr) {
+    if (diag) throw std::logic_error("Unit-triangular matrices support not implemented in trmm()");
+    if (uplo != UpLo::Upper)
+        throw std::logic_error("Left product with lower-triangular matrices not implemented in trmm()");
     int const M = B.first.rows, N = B.first.cols;
     if (A.first.rows != M || A.first.cols != M) throw std::invalid_argument("Matrix sizes do not match");
     if (C.first.rows != M || C.first.cols != N) throw std::invalid_argument("Matrix sizes do not match");
@@ -152,9 +156,12 @@ inline void trmm(double alpha, Batch const& A, UpLo uplo, bool diag, Batch const
                   "trmm");
 }
 
-// C = alpha*B*A, A triangular (algorithm/Trmm.hpp:287-310)
+// C = alpha*B*A, A triangular (algorithm/Trmm.hpp:287-310); BLAST's exceptions kept as above.
 inline void trmm(double alpha, Batch const& B, Batch const& A, UpLo uplo, bool diag, Batch const& C,
                  blastgpu_stream_t stream = nullptr) {
+    if (diag) throw std::logic_error("Unit-triangular matrices support not implemented in trmm()");
+    if (uplo != UpLo::Lower)
+        throw std::logic_error("Right product with upper-triangular matrices not implemented in trmm()");
     int const M = B.first.rows, N = B.first.cols;
     if (A.first.rows != N || A.first.cols != N) throw std::invalid_argument("Matrix sizes do not match");
     if (C.first.rows != M || C.first.cols != N) throw std::invalid_argument("Matrix sizes do not match");

@@ -579,6 +579,56 @@ int oracle_dtrmm(int side, int uplo, int unit, double alpha, oracle_mat A, oracl
     return 0;
 }
 
+int oracle_dtrmm_any(int side, int uplo, int unit, double alpha, oracle_mat A, oracle_mat B, oracle_mat C) {
+    if (!valid(A)) return -5;
+    if (!valid(B)) return -6;
+    if (!valid(C)) return -7;
+    int const M = B.rows, N = B.cols;
+    int const K = side == 0 ? M : N;
+    if (C.rows != M || C.cols != N || A.rows != K || A.cols != K) return -1;
+    Gen a(A), b(B), c(C);
+    auto av = [&](int i, int q) { return (unit && i == q) ? 1.0 : a(i, q); };
+    for (int j = 0; j < N; ++j)
+        for (int i = 0; i < M; ++i) {
+            double acc = 0.0;
+            if (side == 0) {
+                int const q0 = uplo == 1 ? i : 0, q1 = uplo == 1 ? M : i + 1;
+                for (int q = q0; q < q1; ++q) acc = std::fma(alpha * av(i, q), b(q, j), acc);
+            } else {
+                int const q0 = uplo == 1 ? 0 : j, q1 = uplo == 1 ? j + 1 : N;
+                for (int q = q0; q < q1; ++q) acc = std::fma(alpha * b(i, q), av(q, j), acc);
+            }
+            c(i, j) = acc;
+        }
+    return 0;
+}
+
+int oracle_dtrsm_right(int uplo, int unit, int trans_a, oracle_mat A, oracle_mat B, oracle_mat X) {
+    if (!valid(A)) return -4;
+    if (!valid(B)) return -5;
+    if (!valid(X)) return -6;
+    int const M = B.rows, N = B.cols;
+    if (A.rows != N || A.cols != N || X.rows != M || X.cols != N) return -1;
+    Gen a0(A), b(B), x(X);
+    auto a = [&](int q, int j) { return trans_a ? a0(j, q) : a0(q, j); };
+    for (int i = 0; i < M; ++i) {
+        if (uplo == 1) {
+            for (int j = 0; j < N; ++j) {
+                double acc = b(i, j);
+                for (int q = 0; q < j; ++q) acc = std::fma(-x(i, q), a(q, j), acc);
+                x(i, j) = unit ? acc : acc / a(j, j);
+            }
+        } else {
+            for (int j = N; j-- > 0;) {
+                double acc = b(i, j);
+                for (int q = j + 1; q < N; ++q) acc = std::fma(-x(i, q), a(q, j), acc);
+                x(i, j) = unit ? acc : acc / a(j, j);
+            }
+        }
+    }
+    return 0;
+}
+
 int oracle_dpotrs(oracle_mat L, oracle_mat B, oracle_mat X) {
     int const n = L.rows;
     if (L.cols != n || B.rows != n || X.rows != n || X.cols != B.cols) return -1;

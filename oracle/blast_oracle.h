@@ -85,6 +85,16 @@ int oracle_dtrsm(int uplo, int unit, int trans_a, oracle_mat A, oracle_mat B, or
  * Other (side, uplo) pairs and unit diagonals return -100 (BLAST throws std::logic_error). */
 int oracle_dtrmm(int side, int uplo, int unit, double alpha, oracle_mat A, oracle_mat B, oracle_mat C);
 
+/* Variants with no reference algorithm (BLAST throws std::logic_error for them,
+ * algorithm/Trmm.hpp:101-124, 240; RegisterMatrix.hpp:592-597 for the right-side solve). Defined
+ * as the per-element pattern of the implemented ones: trmm accumulates fma(alpha*a_iq, b_qj, .)
+ * (left) or fma(alpha*b_iq, a_qj, .) (right) over the triangle's q range ascending, a unit
+ * diagonal read as 1; the right solve X op(A) = B substitutes column by column (op(A) upper: j
+ * ascending; lower: j descending), acc = fma(-x_iq, a_qj, acc) for q ascending, IEEE division.
+ * oracle_dtrmm_any computes every (side, uplo, unit); uplo of the solve refers to op(A). */
+int oracle_dtrmm_any(int side, int uplo, int unit, double alpha, oracle_mat A, oracle_mat B, oracle_mat C);
+int oracle_dtrsm_right(int uplo, int unit, int trans_a, oracle_mat A, oracle_mat B, oracle_mat X);
+
 /* Composed solves (BLAST has no potrs/getrs; they are trsm sequences):
  * potrs: L*Y = B, L^T*X = Y.   getrs: laswp(B), unit-lower solve, upper solve. X may alias B. */
 int oracle_dpotrs(oracle_mat L, oracle_mat B, oracle_mat X);

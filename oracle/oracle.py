@@ -51,6 +51,8 @@ def lib() -> C.CDLL:
             "oracle_dger": [D, P, I, P, I, M, M],
             "oracle_dtrsm": [I, I, I, M, M, M],
             "oracle_dtrmm": [I, I, I, D, M, M, M],
+            "oracle_dtrmm_any": [I, I, I, D, M, M, M],
+            "oracle_dtrsm_right": [I, I, I, M, M, M],
             "oracle_dpotrs": [M, M, M],
             "oracle_dgetrs": [M, P, M, M],
             "oracle_dposv_batch": [I, I, I64, P, I64, P, P, I64, P, P, I],
@@ -146,6 +148,16 @@ def trsm(uplo: int, unit: int, A, B, X, trans_a: int = 0):
 
 def trmm(side: int, uplo: int, unit: int, alpha, A, B, Cm):
     return lib().oracle_dtrmm(side, uplo, unit, alpha, mat(A), mat(B), mat(Cm))
+
+
+def trmm_any(side: int, uplo: int, unit: int, alpha, A, B, Cm):
+    """Every (side, uplo, unit) trmm, the implemented variants' pattern (no reference algorithm)."""
+    return _check(lib().oracle_dtrmm_any(side, uplo, unit, alpha, mat(A), mat(B), mat(Cm)), "trmm_any")
+
+
+def trsm_right(uplo: int, unit: int, A, B, X, trans_a: int = 0):
+    """X op(A) = B (no reference counterpart; see oracle_dtrsm_right)."""
+    return _check(lib().oracle_dtrsm_right(uplo, unit, trans_a, mat(A), mat(B), mat(X)), "trsm_right")
 
 
 def potrs(L, B, X):

@@ -107,13 +107,65 @@ def test_trmm_sweep_bitexact(gpu, oracle_lib):
                 assert np.array_equal(C2[b], Cr2)
 
 
-def test_trmm_unimplemented_variants(gpu):
-    dA = to_dev(np.eye(3)[None])
-    dB = to_dev(np.ones((1, 3, 3)))
-    dC = gpu.col_major((1,), 3, 3, "cuda")
-    with pytest.raises(NotImplementedError):
-        gpu.trmm(1.0, dA, gpu.LOWER, False, dB, dC)
-    with pytest.raises(NotImplementedError):
-        gpu.trmm(1.0, dB, dA, gpu.UPPER, False, dC)
-    with pytest.raises(NotImplementedError):
-        gpu.trmm(1.0, dA, gpu.UPPER, True, dB, dC)
+@pytest.mark.parametrize("side,uplo,unit", [(0, 0, 0), (0, 0, 1), (0, 1, 1), (1, 1, 0), (1, 1, 1), (1, 0, 1)])
+def test_trmm_variants_blast_leaves_out(gpu, oracle_lib, side, uplo, unit):
+    """The (side, uplo, unit) combinations BLAST throws for (algorithm/Trmm.hpp:101-124, 240):
+    bit for bit against the oracle's extension of the implemented pattern, and against numpy."""
+    import torch
+
+    rng = np.random.default_rng(40 + 4 * side + 2 * uplo + unit)
+    for m in (1, 3, 8, 13, 20):
+        for n in (1, 5, 12, 20):
+            batch = 3
+            k = m if side == 0 else n
+            A = rng.random((batch, k, k))
+            B = rng.random((batch, m, n))
+            alpha = 0.625
+            dA, dB = to_dev(A), to_dev(B)
+            dC = gpu.col_major((batch,), m, n, "cuda")
+            if side == 0:
+                gpu.trmm(alpha, dA, uplo, bool(unit), dB, dC)
+            else:
+                gpu.trmm(alpha, dB, dA, uplo, bool(unit), dC)
+            torch.cuda.synchronize()
+            C = dC.cpu().numpy()
+            for b in range(batch):
+                Cr = F(np.zeros((m, n)))
+                assert oracle_lib.trmm_any(side, uplo, unit, alpha, F(A[b]), F(B[b]), Cr) == 0
+                assert np.array_equal(C[b], Cr), (m, n)
+                T = np.triu(A[b]) if uplo == 1 else np.tril(A[b])
+                if unit:
+                    np.fill_diagonal(T, 1.0)
+                ref = alpha * (T @ B[b] if side == 0 else B[b] @ T)
+                assert approx_equal(C[b], ref, 1e-10, 1e-10)
+
+
+@pytest.mark.parametrize("uplo,unit,trans", [(0, 0, 0), (1, 0, 0), (0, 1, 0), (1, 1, 1), (1, 0, 1)])
+def test_trsm_right_side(gpu, oracle_lib, uplo, unit, trans):
+    """X op(A) = B (no BLAST counterpart), bit for bit against the oracle, residual against numpy."""
+    import torch
+
+    rng = np.random.default_rng(60 + 4 * uplo + 2 * unit + trans)
+    for m in (1, 4, 9, 17):
+        for n in (1, 3, 8, 30):
+            batch = 3
+            A = rng.random((batch, n, n)) + n * np.eye(n)
+            B = rng.random((batch, m, n))
+            dA = to_dev(np.swapaxes(A, 1, 2)).mT if trans else to_dev(A)
+            dB = to_dev(B)
+            dX = gpu.col_major((batch,), m, n, "cuda")
+            gpu.trsm_right(uplo, unit, dA, dB, dX)
+            gpu.trsm_right(uplo, unit, dA, dB, dB)  # X aliasing B
+            torch.cuda.synchronize()
+            X, Xa = dX.cpu().numpy(), dB.cpu().numpy()
+            for b in range(batch):
+                Xr = F(np.zeros((m, n)))
+                At = np.ascontiguousarray(A[b].T) if trans else F(A[b])
+                assert oracle_lib.trsm_right(uplo, unit, At, F(B[b]), Xr, trans) == 0
+                assert np.array_equal(X[b], Xr), (m, n)
+                assert np.array_equal(Xa[b], Xr), (m, n)
+                opA = A[b]
+                T = np.triu(opA) if uplo == 1 else np.tril(opA)
+                if unit:
+                    np.fill_diagonal(T, 1.0)
+                assert approx_equal(X[b] @ T, B[b], 1e-10, 1e-10)
