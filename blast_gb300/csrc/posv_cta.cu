@@ -153,37 +153,47 @@ __device__ __forceinline__ void panel_update_dispatch(T (&acc)[MAXR][4], const T
 }
 
 // Cholesky of the nb x nb diagonal block held in shared memory (column j at blk + j * NMAX),
-// right-looking, all threads: step j takes the pivot d = a_jj, y = 1/sqrt(d), and updates the
-// trailing block a_il = fma(-(a_ij*y), (a_lj*y), a_il) (warp w: columns l = j+1+w, j+1+w+8, ...;
-// lane: row l + lane); column j itself is scaled during step j+1, when nobody reads it any more.
-// One barrier per step. rinv[j] = y. Records the first bad pivot (k0 + j + 1) in *s_info.
+// right-looking, all threads. Column j is final (scaled) before step j: step j updates the
+// trailing block a_il = fma(-l_ij, l_lj, a_il) (warp w: columns l = j+1+w, j+1+w+8, ...; lane: row
+// l + lane), and warp 0, which owns column j+1, finishes it in the same step: the new pivot
+// d = a_{j+1,j+1} comes from lane 0 by a shuffle, y = 1/sqrt(d), and the column is stored as
+// a_{i,j+1} * y. Every element is then a single fused multiply-add per step, the reciprocal
+// square root is taken by one warp, and there is one barrier per column. The products equal
+// RegisterMatrix::potrf's (the pivot column scaled by 1/sqrt(d) once, then used unrounded).
+// rinv[j] = 1/l_jj. Records the first bad pivot (k0 + j + 1) in *s_info.
 template <typename T, int NMAX>
 __device__ __forceinline__ void cta_chol_block(T* blk, int nb, int k0, T* rinv, int* s_info) {
     int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    T dprev = (T)1, yprev = (T)1;
-    for (int j = 0; j < nb; ++j) {
-        T const d = blk[j * NMAX + j];
+    if (warp == 0) {
+        T const v = lane < nb ? blk[lane] : (T)0;
+        T const d = __shfl_sync(0xffffffffu, v, 0);
         T const y = rsqrt_t<T>(d);
-        if (tid == 0) {
-            if (!(d > (T)0) && *s_info == 0) *s_info = k0 + j + 1;
-            rinv[j] = y;
+        if (lane == 0) {
+            if (!(d > (T)0) && *s_info == 0) *s_info = k0 + 1;
+            rinv[0] = y;
         }
-        if (j > 0 && tid < nb - (j - 1)) {
-            int const i = j - 1 + tid;
-            T* c = blk + (j - 1) * NMAX;
-            c[i] = i == j - 1 ? dprev * yprev : c[i] * yprev;
-        }
+        if (lane < nb) blk[lane] = v * y;
+    }
+    __syncthreads();
+    for (int j = 0; j + 1 < nb; ++j) {
         T const* cj = blk + j * NMAX;
         for (int l = j + 1 + warp; l < nb; l += kWarps) {
             int const i = l + lane;
-            if (i < nb) blk[l * NMAX + i] = fma(-(cj[i] * y), cj[l] * y, blk[l * NMAX + i]);
+            T const v = i < nb ? fma(-cj[i], cj[l], blk[l * NMAX + i]) : (T)0;
+            if (l == j + 1) {  // warp 0: the next pivot column
+                T const d = __shfl_sync(0xffffffffu, v, 0);
+                T const y = rsqrt_t<T>(d);
+                if (lane == 0) {
+                    if (!(d > (T)0) && *s_info == 0) *s_info = k0 + j + 2;
+                    rinv[j + 1] = y;
+                }
+                if (i < nb) blk[l * NMAX + i] = v * y;
+            } else if (i < nb) {
+                blk[l * NMAX + i] = v;
+            }
         }
-        dprev = d;
-        yprev = y;
         __syncthreads();
     }
-    if (nb > 0 && tid < 1) blk[(nb - 1) * NMAX + (nb - 1)] = dprev * yprev;
-    __syncthreads();
 }
 
 // Left-looking blocked Cholesky of the n x n matrix: lower(A) -> F (precision T, ld ldf).
