@@ -320,14 +320,38 @@ __device__ void getrs_thread(int n, int nrhs, const double* a, int lda, const in
                 xj[q] = t;
             }
         }
+        // The dot products keep BLAST's ascending order; each pass of 16 issues its 32 loads before
+        // the 16 dependent fused multiply-adds, so the thread waits for memory once per 16 terms.
         for (int i = 0; i < n; ++i) {
             double acc = xj[i];
-            for (int k = 0; k < i; ++k) acc = fma(-a[i + (int64_t)k * lda], xj[k], acc);
+            int k = 0;
+            for (; k + 16 <= i; k += 16) {
+                double av[16], xv[16];
+#pragma unroll
+                for (int u = 0; u < 16; ++u) {
+                    av[u] = a[i + (int64_t)(k + u) * lda];
+                    xv[u] = xj[k + u];
+                }
+#pragma unroll
+                for (int u = 0; u < 16; ++u) acc = fma(-av[u], xv[u], acc);
+            }
+            for (; k < i; ++k) acc = fma(-a[i + (int64_t)k * lda], xj[k], acc);
             xj[i] = acc;
         }
         for (int i = n; i-- > 0;) {
             double acc = xj[i];
-            for (int k = i + 1; k < n; ++k) acc = fma(-a[i + (int64_t)k * lda], xj[k], acc);
+            int k = i + 1;
+            for (; k + 16 <= n; k += 16) {
+                double av[16], xv[16];
+#pragma unroll
+                for (int u = 0; u < 16; ++u) {
+                    av[u] = a[i + (int64_t)(k + u) * lda];
+                    xv[u] = xj[k + u];
+                }
+#pragma unroll
+                for (int u = 0; u < 16; ++u) acc = fma(-av[u], xv[u], acc);
+            }
+            for (; k < n; ++k) acc = fma(-a[i + (int64_t)k * lda], xj[k], acc);
             xj[i] = acc / a[i + (int64_t)i * lda];
         }
     }
