@@ -67,6 +67,8 @@ SIGNATURES: dict[str, list] = {
                                      I64, PTR],
     "blastgpu_dtrsm_right_strided": [I32, I32, I32, I32, I32, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, I64,
                                      PTR],
+    "blastgpu_dgetrs_interleave_plan": [PTR, PTR, I64, PTR],
+    "blastgpu_dgetrs_batched_ws": [PTR, PTR, I64, PTR, PTR, PTR],
     "blastgpu_dger_strided": [I32, I32, DBL, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, I64, PTR],
     "blastgpu_idamax_strided": [I32, PTR, I32, I64, PTR, I64, PTR],
     "blastgpu_dlaswp_strided": [I32, PTR, I32, I64, I32, I32, PTR, I64, I64, PTR],
@@ -86,7 +88,8 @@ SIGNATURES: dict[str, list] = {
     "blastgpu_dposv_mixed_batched_noalloc": [PTR, I64, I32, C.c_size_t, DBL, I32, PTR, PTR, PTR, PTR],
 }
 _RESTYPES = {"blastgpu_status_string": C.c_char_p, "blastgpu_launch_count": C.c_int64,
-             "blastgpu_dposv_mixed_workspace_bytes": C.c_size_t}
+             "blastgpu_dposv_mixed_workspace_bytes": C.c_size_t,
+             "blastgpu_dgetrs_interleave_plan": C.c_int64}
 
 
 def lib() -> C.CDLL:

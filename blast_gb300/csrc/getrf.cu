@@ -395,6 +395,116 @@ __global__ void __launch_bounds__(128) getrs_thread_kernel(Batch batch, int64_t 
     getrs_thread(it.n, it.nrhs, it.a, it.lda, it.ipiv, it.x, it.ldx);
 }
 
+// Lane-interleaved getrs. Thread-per-matrix solves read a different matrix in every lane, so each
+// load instruction touches 32 unrelated sectors and the chains stall on memory. The interleaved
+// path first copies each group of 32 consecutive instances into a workspace region where element
+// (i, k) of instance 32w + l sits at off_w + (k * nmax_w + i) * 32 + l (nmax_w: the group's largest
+// n), then solves with the same per-thread chains in BLAST's order, now reading 256 contiguous
+// bytes per warp load. The right-hand sides follow at off_w + 32 nmax_w^2 + (j * nmax_w + k) * 32 + l.
+__device__ __forceinline__ int group_nmax(DescGetrs const& batch, int64_t count, int64_t b0, int lane, int& n_own,
+                                          int& r_max) {
+    int n = 0, r = 0;
+    if (b0 + lane < count) {
+        blastgpu_getrf_desc const& d = batch.desc[b0 + lane];
+        n = d.A.rows;
+        r = d.B.cols;
+    }
+    n_own = n;
+    int nm = n;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        nm = max(nm, __shfl_xor_sync(0xffffffffu, nm, off));
+        r = max(r, __shfl_xor_sync(0xffffffffu, r, off));
+    }
+    r_max = r;
+    return nm;
+}
+
+// One CTA (8 warps) per group of 32 instances: warp w copies rows i = w, w+8, ... of every column,
+// lane l taking instance 32g + l (the 8 warps together read 8 consecutive rows of a column, so the
+// sectors are shared through L1); stores are 256 contiguous bytes per warp.
+__global__ void __launch_bounds__(256) getrs_interleave_kernel(DescGetrs batch, int64_t count, const int64_t* offsets,
+                                                               double* ws) {
+    int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int64_t const b0 = (int64_t)blockIdx.x * 32;
+    int n_own, r_max;
+    int const nmax = group_nmax(batch, count, b0, lane, n_own, r_max);
+    double* dst = ws + offsets[blockIdx.x];
+    const double* a = nullptr;
+    int lda = 1;
+    if (n_own > 0) {
+        blastgpu_getrf_desc const& d = batch.desc[b0 + lane];
+        a = d.A.data;
+        lda = d.A.ld;
+    }
+    for (int k = 0; k < nmax; ++k)
+        for (int i = warp; i < nmax; i += 8)
+            dst[((int64_t)k * nmax + i) * 32 + lane] = (i < n_own && k < n_own) ? a[i + (int64_t)k * lda] : 0.0;
+}
+
+// Thread per instance on the interleaved copy: laswp, unit-lower and upper substitution in
+// BLAST's order (identical chains to getrs_thread), 16 loads issued ahead of their FMAs.
+__global__ void __launch_bounds__(32) getrs_interleaved_kernel(DescGetrs batch, int64_t count, const int32_t* info,
+                                                               const int64_t* offsets, double* ws) {
+    int const lane = threadIdx.x;
+    int64_t const b0 = (int64_t)blockIdx.x * 32;
+    int n, r_max;
+    int const nmax = group_nmax(batch, count, b0, lane, n, r_max);
+    if (n == 0) return;
+    if (info && info[b0 + lane] != 0) return;  // singular factor: BLAST would have thrown in getrf
+    GetrsItem const it = batch.get(b0 + lane);
+    const double* A = ws + offsets[blockIdx.x];
+    double* X = ws + offsets[blockIdx.x] + (int64_t)32 * nmax * nmax;
+    auto a = [&](int i, int k) -> double { return A[((int64_t)k * nmax + i) * 32 + lane]; };
+    for (int j = 0; j < it.nrhs; ++j) {
+        double* x = X + (int64_t)j * nmax * 32 + lane;  // x[k * 32]
+        const double* bj = it.x + (int64_t)j * it.ldx;
+        for (int k = 0; k < n; ++k) x[k * 32] = bj[k];
+        for (int k = 0; k < n; ++k) {
+            int const q = it.ipiv[k];
+            if (q != k) {
+                double const t = x[k * 32];
+                x[k * 32] = x[q * 32];
+                x[q * 32] = t;
+            }
+        }
+        for (int i = 0; i < n; ++i) {
+            double acc = x[i * 32];
+            int k = 0;
+            for (; k + 16 <= i; k += 16) {
+                double av[16], xv[16];
+#pragma unroll
+                for (int u = 0; u < 16; ++u) {
+                    av[u] = a(i, k + u);
+                    xv[u] = x[(k + u) * 32];
+                }
+#pragma unroll
+                for (int u = 0; u < 16; ++u) acc = fma(-av[u], xv[u], acc);
+            }
+            for (; k < i; ++k) acc = fma(-a(i, k), x[k * 32], acc);
+            x[i * 32] = acc;
+        }
+        for (int i = n; i-- > 0;) {
+            double acc = x[i * 32];
+            int k = i + 1;
+            for (; k + 16 <= n; k += 16) {
+                double av[16], xv[16];
+#pragma unroll
+                for (int u = 0; u < 16; ++u) {
+                    av[u] = a(i, k + u);
+                    xv[u] = x[(k + u) * 32];
+                }
+#pragma unroll
+                for (int u = 0; u < 16; ++u) acc = fma(-av[u], xv[u], acc);
+            }
+            for (; k < n; ++k) acc = fma(-a(i, k), x[k * 32], acc);
+            x[i * 32] = acc / a(i, i);
+        }
+        double* out = it.x + (int64_t)j * it.ldx;
+        for (int k = 0; k < n; ++k) out[k] = x[k * 32];
+    }
+}
+
 // "getrf.cta.n<bin>" = 1 selects the CTA-per-matrix kernel for that size bin; by default it is
 // used above n = 64, the warp-per-matrix kernel below.
 template <class Batch>
@@ -453,6 +563,42 @@ int blastgpu_dgetrf_batched(const blastgpu_getrf_desc* desc, int32_t* info, int6
     if (!desc) return -1;
     if (max_n < 0) return -4;
     return launch_getrf(DescGetrf{desc}, batch, max_n, info, as_cuda(stream));
+}
+
+int64_t blastgpu_dgetrs_interleave_plan(const int32_t* n, const int32_t* nrhs, int64_t batch, int64_t* offsets) {
+    if (batch < 0 || (batch > 0 && (!n || !nrhs))) return -1;
+    int64_t const groups = (batch + 31) / 32;
+    int64_t total = 0;
+    for (int64_t g = 0; g < groups; ++g) {
+        int64_t nm = 0, rm = 0;
+        for (int64_t b = 32 * g; b < batch && b < 32 * g + 32; ++b) {
+            if (n[b] < 0 || nrhs[b] < 0) return -1;
+            nm = n[b] > nm ? n[b] : nm;
+            rm = nrhs[b] > rm ? nrhs[b] : rm;
+        }
+        if (offsets) offsets[g] = total;
+        total += 32 * (nm * nm + nm * rm);
+    }
+    if (offsets) offsets[groups] = total;
+    return total * (int64_t)sizeof(double);
+}
+
+int blastgpu_dgetrs_batched_ws(const blastgpu_getrf_desc* desc, const int32_t* info, int64_t batch,
+                               const int64_t* offsets, double* workspace, blastgpu_stream_t stream) {
+    if (batch < 0) return -3;
+    if (batch == 0) return BLASTGPU_SUCCESS;
+    if (!desc) return -1;
+    if (!offsets) return -4;
+    if (!workspace) return -5;
+    int64_t const groups = (batch + 31) / 32;
+    if (groups > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
+    cudaStream_t const s = as_cuda(stream);
+    DescGetrs const d{desc};
+    getrs_interleave_kernel<<<(unsigned)groups, 256, 0, s>>>(d, batch, offsets, workspace);
+    int st = check_launch();
+    if (st != BLASTGPU_SUCCESS) return st;
+    getrs_interleaved_kernel<<<(unsigned)groups, 32, 0, s>>>(d, batch, info, offsets, workspace);
+    return check_launch();
 }
 
 int blastgpu_dgetrs_strided(int n, int nrhs, const double* LU, int lda, int64_t stride_a,

@@ -132,3 +132,70 @@ def test_gesv_ragged_log_uniform(gpu, oracle_lib):
         xr = np.asfortranarray(b.copy())
         oracle_lib.getrs(LUr, pr, xr, xr)
         assert np.array_equal(dB.cpu().numpy(), xr), n
+
+
+def test_getrs_interleaved_matches_oracle(gpu, oracle_lib):
+    """blastgpu_dgetrs_batched_ws (lane-interleaved copy of the factors): unsorted ragged sizes,
+    several right-hand sides, groups that end part-way; bit-identical to the oracle's getrs."""
+    import torch
+
+    from blast_gb300 import _lib, desc
+
+    rng = np.random.default_rng(77)
+    count = 75
+    ns = rng.integers(1, 140, count)
+    rs = rng.integers(1, 4, count)
+    As = [rng.standard_normal((n, n)) for n in ns]
+    Bs = [rng.standard_normal((n, r)) for n, r in zip(ns, rs)]
+    recs = np.zeros(count, dtype=desc.GETRF_DTYPE)
+    keep = []
+    for i, (n, A, B) in enumerate(zip(ns, As, Bs)):
+        LUr, pr, _ = _oracle_lu(oracle_lib, A)
+        dA, dB = to_dev(LUr), to_dev(B)
+        p = torch.from_numpy(pr).cuda()
+        recs[i] = (desc.mat_record(dA), p.data_ptr(), desc.mat_record(dB))
+        keep.append((LUr, pr, dB, p, dA))
+    d = desc.upload(recs, "cuda")
+    n32, r32 = ns.astype(np.int32), rs.astype(np.int32)
+    offs = np.zeros((count + 31) // 32 + 1, dtype=np.int64)
+    nbytes = _lib.lib().blastgpu_dgetrs_interleave_plan(n32.ctypes.data, r32.ctypes.data, count, offs.ctypes.data)
+    assert nbytes == offs[-1] * 8 > 0
+    dOffs = torch.from_numpy(offs).cuda()
+    ws = torch.full((nbytes // 8,), float("nan"), dtype=torch.float64, device="cuda")
+    info = torch.zeros(count, dtype=torch.int32, device="cuda")
+    _lib.call("blastgpu_dgetrs_batched_ws", d.data_ptr(), info.data_ptr(), count, dOffs.data_ptr(),
+              ws.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    for (LUr, pr, dB, p, dA), B in zip(keep, Bs):
+        Xr = np.asfortranarray(B.copy())
+        oracle_lib.getrs(LUr, pr, Xr, Xr)
+        assert np.array_equal(dB.cpu().numpy(), Xr)
+    assert _lib.lib().blastgpu_dgetrs_interleave_plan(n32.ctypes.data, r32.ctypes.data, -1, None) == -1
+
+
+def test_gesv_plan_log_uniform(gpu, oracle_lib):
+    """GesvPlan (two getrf bins on forked streams, then the interleaved getrs) on the ragged LU
+    workload's size distribution: pivots and solutions bit-identical to the oracle."""
+    import torch
+
+    from blast_gb300.ragged import GesvPlan, Packed
+
+    rng = np.random.default_rng(2027)
+    count = 200
+    ns = np.floor(np.exp(rng.uniform(np.log(4), np.log(257), count))).astype(int)
+    As = [rng.standard_normal((n, n)) for n in ns]
+    bs = [rng.standard_normal((n, 1)) for n in ns]
+    A = Packed(ns, ns, "cuda")
+    A.fill_from(As)
+    B = Packed(ns, np.ones_like(ns), "cuda")
+    B.fill_from(bs)
+    gp = GesvPlan(A, B)
+    gp.run()
+    torch.cuda.synchronize()
+    assert not gp.info_host().any()
+    for n, A0, b, x, p in zip(ns, As, bs, B.to_list(), gp.pivots()):
+        LUr, pr, _ = _oracle_lu(oracle_lib, A0)
+        xr = np.asfortranarray(b.copy())
+        oracle_lib.getrs(LUr, pr, xr, xr)
+        assert np.array_equal(p, pr), n
+        assert np.array_equal(x, xr), n
