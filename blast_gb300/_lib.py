@@ -67,8 +67,6 @@ SIGNATURES: dict[str, list] = {
                                      I64, PTR],
     "blastgpu_dtrsm_right_strided": [I32, I32, I32, I32, I32, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, I64,
                                      PTR],
-    "blastgpu_dgetrs_interleave_plan": [PTR, PTR, I64, PTR],
-    "blastgpu_dgetrs_batched_ws": [PTR, PTR, I64, PTR, PTR, PTR],
     "blastgpu_dger_strided": [I32, I32, DBL, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, I64, PTR],
     "blastgpu_idamax_strided": [I32, PTR, I32, I64, PTR, I64, PTR],
     "blastgpu_dlaswp_strided": [I32, PTR, I32, I64, I32, I32, PTR, I64, I64, PTR],
@@ -76,7 +74,7 @@ SIGNATURES: dict[str, list] = {
     "blastgpu_dgetrf_strided": [I32, I32, PTR, I32, I64, PTR, I64, PTR, I64, PTR],
     "blastgpu_dgetrs_strided": [I32, I32, PTR, I32, I64, PTR, I64, PTR, I32, I64, PTR, I64, PTR],
     "blastgpu_dgetrf_batched": [PTR, PTR, I64, I32, PTR],
-    "blastgpu_dgetrs_batched": [PTR, PTR, I64, PTR],
+    "blastgpu_dgetrs_batched": [PTR, PTR, I64, I32, PTR],
     "blastgpu_dgesv_batched": [PTR, PTR, I64, I32, PTR],
     "blastgpu_dposv_mixed_workspace_bytes": [I32],
     "blastgpu_dsyrk_lower_strided": [I32, I32, DBL, PTR, I32, I64, DBL, PTR, I32, I64, PTR, I32, I64, I64, PTR],
@@ -88,8 +86,7 @@ SIGNATURES: dict[str, list] = {
     "blastgpu_dposv_mixed_batched_noalloc": [PTR, I64, I32, C.c_size_t, DBL, I32, PTR, PTR, PTR, PTR],
 }
 _RESTYPES = {"blastgpu_status_string": C.c_char_p, "blastgpu_launch_count": C.c_int64,
-             "blastgpu_dposv_mixed_workspace_bytes": C.c_size_t,
-             "blastgpu_dgetrs_interleave_plan": C.c_int64}
+             "blastgpu_dposv_mixed_workspace_bytes": C.c_size_t}
 
 
 def lib() -> C.CDLL:

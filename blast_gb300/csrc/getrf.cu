@@ -19,6 +19,8 @@
 //  * getrs: one thread per matrix. The backward substitution is a chain of dependent dot
 //    products in BLAST's order (each x_i starts from x_{i+1}); running whole solves per thread
 //    keeps every lane busy while preserving that order.
+#include <atomic>
+
 #include "common.cuh"
 
 namespace blastgpu {
@@ -305,58 +307,6 @@ __global__ void __launch_bounds__(kWarps * 32) getrf_warp_kernel(Batch batch, in
     if (info && lane == 0) info[b] = r;
 }
 
-// getrs for one matrix and its right-hand sides, in BLAST's scalar order (dense/Trsm.hpp:39-65):
-// laswp(b) with ipiv[0..n), x_i = b_i - sum_{k<i} l_ik x_k (unit lower), then
-// x_i = (x_i - sum_{k>i, ascending} u_ik x_k) / u_ii.
-__device__ void getrs_thread(int n, int nrhs, const double* a, int lda, const int32_t* ipiv,
-                             double* x, int ldx) {
-    for (int j = 0; j < nrhs; ++j) {
-        double* xj = x + (int64_t)j * ldx;
-        for (int k = 0; k < n; ++k) {
-            int const q = ipiv[k];
-            if (q != k) {
-                double const t = xj[k];
-                xj[k] = xj[q];
-                xj[q] = t;
-            }
-        }
-        // The dot products keep BLAST's ascending order; each pass of 16 issues its 32 loads before
-        // the 16 dependent fused multiply-adds, so the thread waits for memory once per 16 terms.
-        for (int i = 0; i < n; ++i) {
-            double acc = xj[i];
-            int k = 0;
-            for (; k + 16 <= i; k += 16) {
-                double av[16], xv[16];
-#pragma unroll
-                for (int u = 0; u < 16; ++u) {
-                    av[u] = a[i + (int64_t)(k + u) * lda];
-                    xv[u] = xj[k + u];
-                }
-#pragma unroll
-                for (int u = 0; u < 16; ++u) acc = fma(-av[u], xv[u], acc);
-            }
-            for (; k < i; ++k) acc = fma(-a[i + (int64_t)k * lda], xj[k], acc);
-            xj[i] = acc;
-        }
-        for (int i = n; i-- > 0;) {
-            double acc = xj[i];
-            int k = i + 1;
-            for (; k + 16 <= n; k += 16) {
-                double av[16], xv[16];
-#pragma unroll
-                for (int u = 0; u < 16; ++u) {
-                    av[u] = a[i + (int64_t)(k + u) * lda];
-                    xv[u] = xj[k + u];
-                }
-#pragma unroll
-                for (int u = 0; u < 16; ++u) acc = fma(-av[u], xv[u], acc);
-            }
-            for (; k < n; ++k) acc = fma(-a[i + (int64_t)k * lda], xj[k], acc);
-            xj[i] = acc / a[i + (int64_t)i * lda];
-        }
-    }
-}
-
 struct GetrsItem {
     const double* a;
     int n, lda;
@@ -386,78 +336,38 @@ struct DescGetrs {
     }
 };
 
+// getrs, one thread per instance, in BLAST's scalar order (dense/Trsm.hpp:39-65): laswp(b) with
+// ipiv[0..n), x_i = b_i - sum_{k<i} l_ik x_k (unit lower), x_i = (x_i - sum_{k>i} u_ik x_k) / u_ii,
+// every sum in ascending k. The solution vector lives in shared memory (x[k * 32 + lane], max_n * 32
+// doubles per warp). A dependent binary64 FMA chain is latency-bound on GB300, so the forward solve
+// runs four rows' chains side by side (each still in ascending k); the backward chain is inherently
+// serial in BLAST's order (row i starts from x_{i+1}). Factor terms are loaded a pass ahead of the
+// FMAs that use them (forward: 4 rows x 8 terms; backward: 16 terms along the row, the next row's
+// first pass and diagonal included), so memory latency overlaps the chain. A short pass reads
+// zeros past the row's end and skips their FMAs.
+struct FactorView {
+    const double* p;
+    int64_t ld;
+    __device__ __forceinline__ double operator()(int i, int k) const { return p[i + k * ld]; }
+};
+
+__device__ __forceinline__ void load_pass(FactorView const& A, int i, int k0, int k1, double (&av)[16]) {
+#pragma unroll
+    for (int u = 0; u < 16; ++u) av[u] = k0 + u < k1 ? A(i, k0 + u) : 0.0;
+}
+
 template <class Batch>
-__global__ void __launch_bounds__(128) getrs_thread_kernel(Batch batch, int64_t count, const int32_t* info) {
-    int64_t const b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(32) getrs_kernel(Batch batch, int64_t count, const int32_t* info) {
+    extern __shared__ double xs[];
+    int const lane = threadIdx.x;
+    int64_t const b = (int64_t)blockIdx.x * 32 + lane;
     if (b >= count) return;
     if (info && info[b] != 0) return;  // singular factor: BLAST would have thrown in getrf
     GetrsItem const it = batch.get(b);
-    getrs_thread(it.n, it.nrhs, it.a, it.lda, it.ipiv, it.x, it.ldx);
-}
-
-// Lane-interleaved getrs. Thread-per-matrix solves read a different matrix in every lane, so each
-// load instruction touches 32 unrelated sectors and the chains stall on memory. The interleaved
-// path first copies each group of 32 consecutive instances into a workspace region where element
-// (i, k) of instance 32w + l sits at off_w + (k * nmax_w + i) * 32 + l (nmax_w: the group's largest
-// n), then solves with the same per-thread chains in BLAST's order, now reading 256 contiguous
-// bytes per warp load. The right-hand sides follow at off_w + 32 nmax_w^2 + (j * nmax_w + k) * 32 + l.
-__device__ __forceinline__ int group_nmax(DescGetrs const& batch, int64_t count, int64_t b0, int lane, int& n_own,
-                                          int& r_max) {
-    int n = 0, r = 0;
-    if (b0 + lane < count) {
-        blastgpu_getrf_desc const& d = batch.desc[b0 + lane];
-        n = d.A.rows;
-        r = d.B.cols;
-    }
-    n_own = n;
-    int nm = n;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        nm = max(nm, __shfl_xor_sync(0xffffffffu, nm, off));
-        r = max(r, __shfl_xor_sync(0xffffffffu, r, off));
-    }
-    r_max = r;
-    return nm;
-}
-
-// One CTA (8 warps) per group of 32 instances: warp w copies rows i = w, w+8, ... of every column,
-// lane l taking instance 32g + l (the 8 warps together read 8 consecutive rows of a column, so the
-// sectors are shared through L1); stores are 256 contiguous bytes per warp.
-__global__ void __launch_bounds__(256) getrs_interleave_kernel(DescGetrs batch, int64_t count, const int64_t* offsets,
-                                                               double* ws) {
-    int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int64_t const b0 = (int64_t)blockIdx.x * 32;
-    int n_own, r_max;
-    int const nmax = group_nmax(batch, count, b0, lane, n_own, r_max);
-    double* dst = ws + offsets[blockIdx.x];
-    const double* a = nullptr;
-    int lda = 1;
-    if (n_own > 0) {
-        blastgpu_getrf_desc const& d = batch.desc[b0 + lane];
-        a = d.A.data;
-        lda = d.A.ld;
-    }
-    for (int k = 0; k < nmax; ++k)
-        for (int i = warp; i < nmax; i += 8)
-            dst[((int64_t)k * nmax + i) * 32 + lane] = (i < n_own && k < n_own) ? a[i + (int64_t)k * lda] : 0.0;
-}
-
-// Thread per instance on the interleaved copy: laswp, unit-lower and upper substitution in
-// BLAST's order (identical chains to getrs_thread), 16 loads issued ahead of their FMAs.
-__global__ void __launch_bounds__(32) getrs_interleaved_kernel(DescGetrs batch, int64_t count, const int32_t* info,
-                                                               const int64_t* offsets, double* ws) {
-    int const lane = threadIdx.x;
-    int64_t const b0 = (int64_t)blockIdx.x * 32;
-    int n, r_max;
-    int const nmax = group_nmax(batch, count, b0, lane, n, r_max);
-    if (n == 0) return;
-    if (info && info[b0 + lane] != 0) return;  // singular factor: BLAST would have thrown in getrf
-    GetrsItem const it = batch.get(b0 + lane);
-    const double* A = ws + offsets[blockIdx.x];
-    double* X = ws + offsets[blockIdx.x] + (int64_t)32 * nmax * nmax;
-    auto a = [&](int i, int k) -> double { return A[((int64_t)k * nmax + i) * 32 + lane]; };
+    int const n = it.n;
+    FactorView const A{it.a, it.lda};
+    double* x = xs + lane;  // x[k * 32]
     for (int j = 0; j < it.nrhs; ++j) {
-        double* x = X + (int64_t)j * nmax * 32 + lane;  // x[k * 32]
         const double* bj = it.x + (int64_t)j * it.ldx;
         for (int k = 0; k < n; ++k) x[k * 32] = bj[k];
         for (int k = 0; k < n; ++k) {
@@ -468,37 +378,70 @@ __global__ void __launch_bounds__(32) getrs_interleaved_kernel(DescGetrs batch, 
                 x[q * 32] = t;
             }
         }
-        for (int i = 0; i < n; ++i) {
-            double acc = x[i * 32];
-            int k = 0;
-            for (; k + 16 <= i; k += 16) {
-                double av[16], xv[16];
+        for (int i0 = 0; i0 < n; i0 += 4) {
+            double acc[4];
 #pragma unroll
-                for (int u = 0; u < 16; ++u) {
-                    av[u] = a(i, k + u);
-                    xv[u] = x[(k + u) * 32];
+            for (int r = 0; r < 4; ++r) acc[r] = i0 + r < n ? x[(i0 + r) * 32] : 0.0;
+            double av[4][8];
+            auto load8 = [&](int k0, double (&dst)[4][8]) {
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) dst[r][u] = (i0 + r < n && k0 + u < i0) ? A(i0 + r, k0 + u) : 0.0;
+            };
+            if (i0 > 0) load8(0, av);
+            for (int k0 = 0; k0 < i0; k0 += 8) {
+                double an[4][8];
+                if (k0 + 8 < i0) load8(k0 + 8, an);
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    if (k0 + u < i0) {
+                        double const xk = x[(k0 + u) * 32];
+#pragma unroll
+                        for (int r = 0; r < 4; ++r) acc[r] = fma(-av[r][u], xk, acc[r]);
+                    }
                 }
 #pragma unroll
-                for (int u = 0; u < 16; ++u) acc = fma(-av[u], xv[u], acc);
+                for (int r = 0; r < 4; ++r)
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) av[r][u] = an[r][u];
             }
-            for (; k < i; ++k) acc = fma(-a(i, k), x[k * 32], acc);
-            x[i * 32] = acc;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                int const i = i0 + r;
+                if (i < n) {
+#pragma unroll
+                    for (int q = 0; q < r; ++q) acc[r] = fma(-A(i, i0 + q), x[(i0 + q) * 32], acc[r]);
+                    x[i * 32] = acc[r];
+                }
+            }
         }
-        for (int i = n; i-- > 0;) {
-            double acc = x[i * 32];
-            int k = i + 1;
-            for (; k + 16 <= n; k += 16) {
-                double av[16], xv[16];
-#pragma unroll
-                for (int u = 0; u < 16; ++u) {
-                    av[u] = a(i, k + u);
-                    xv[u] = x[(k + u) * 32];
+        {
+            int i = n - 1, k0 = n;
+            double av[16], acc = 0.0;
+            load_pass(A, i, k0, n, av);
+            double d = A(i, i);
+            while (i >= 0) {
+                int ni = i, nk = k0 + 16;
+                if (nk >= n) { ni = i - 1; nk = i; }
+                double an[16], dn = 0.0;
+                if (ni >= 0) {
+                    load_pass(A, ni, nk, n, an);
+                    if (ni != i) dn = A(ni, ni);
                 }
+                if (k0 == i + 1) acc = x[i * 32];
 #pragma unroll
-                for (int u = 0; u < 16; ++u) acc = fma(-av[u], xv[u], acc);
+                for (int u = 0; u < 16; ++u)
+                    if (k0 + u < n) acc = fma(-av[u], x[(k0 + u) * 32], acc);
+                if (ni != i) {
+                    x[i * 32] = acc / d;
+                    d = dn;
+                }
+                i = ni;
+                k0 = nk;
+#pragma unroll
+                for (int u = 0; u < 16; ++u) av[u] = an[u];
             }
-            for (; k < n; ++k) acc = fma(-a(i, k), x[k * 32], acc);
-            x[i * 32] = acc / a(i, i);
         }
         double* out = it.x + (int64_t)j * it.ldx;
         for (int k = 0; k < n; ++k) out[k] = x[k * 32];
@@ -521,11 +464,23 @@ int launch_getrf(Batch const& batch, int64_t count, int max_n, int32_t* info, cu
     return check_launch();
 }
 
+// max_n bounds every instance's n; the solution vectors of a warp's 32 instances take
+// 32 * max_n doubles of shared memory (n up to 800).
 template <class Batch>
-int launch_getrs(Batch const& batch, int64_t count, const int32_t* info, cudaStream_t s) {
-    int64_t const blocks = (count + 127) / 128;
+int launch_getrs(Batch const& batch, int64_t count, int max_n, const int32_t* info, cudaStream_t s) {
+    if (count == 0 || max_n == 0) return BLASTGPU_SUCCESS;
+    int64_t const blocks = (count + 31) / 32;
     if (blocks > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
-    getrs_thread_kernel<<<(unsigned)blocks, 128, 0, s>>>(batch, count, info);
+    size_t const smem = sizeof(double) * 32 * (size_t)max_n;
+    if (smem > 200 * 1024) return BLASTGPU_ERR_TOO_LARGE;
+    static std::atomic<size_t> smem_set{0};
+    if (smem > 48 * 1024 && smem_set.load() < smem) {
+        cudaError_t const e =
+            cudaFuncSetAttribute(getrs_kernel<Batch>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
+        smem_set.store(200 * 1024);
+    }
+    getrs_kernel<Batch><<<(unsigned)blocks, 32, smem, s>>>(batch, count, info);
     return check_launch();
 }
 
@@ -565,42 +520,6 @@ int blastgpu_dgetrf_batched(const blastgpu_getrf_desc* desc, int32_t* info, int6
     return launch_getrf(DescGetrf{desc}, batch, max_n, info, as_cuda(stream));
 }
 
-int64_t blastgpu_dgetrs_interleave_plan(const int32_t* n, const int32_t* nrhs, int64_t batch, int64_t* offsets) {
-    if (batch < 0 || (batch > 0 && (!n || !nrhs))) return -1;
-    int64_t const groups = (batch + 31) / 32;
-    int64_t total = 0;
-    for (int64_t g = 0; g < groups; ++g) {
-        int64_t nm = 0, rm = 0;
-        for (int64_t b = 32 * g; b < batch && b < 32 * g + 32; ++b) {
-            if (n[b] < 0 || nrhs[b] < 0) return -1;
-            nm = n[b] > nm ? n[b] : nm;
-            rm = nrhs[b] > rm ? nrhs[b] : rm;
-        }
-        if (offsets) offsets[g] = total;
-        total += 32 * (nm * nm + nm * rm);
-    }
-    if (offsets) offsets[groups] = total;
-    return total * (int64_t)sizeof(double);
-}
-
-int blastgpu_dgetrs_batched_ws(const blastgpu_getrf_desc* desc, const int32_t* info, int64_t batch,
-                               const int64_t* offsets, double* workspace, blastgpu_stream_t stream) {
-    if (batch < 0) return -3;
-    if (batch == 0) return BLASTGPU_SUCCESS;
-    if (!desc) return -1;
-    if (!offsets) return -4;
-    if (!workspace) return -5;
-    int64_t const groups = (batch + 31) / 32;
-    if (groups > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
-    cudaStream_t const s = as_cuda(stream);
-    DescGetrs const d{desc};
-    getrs_interleave_kernel<<<(unsigned)groups, 256, 0, s>>>(d, batch, offsets, workspace);
-    int st = check_launch();
-    if (st != BLASTGPU_SUCCESS) return st;
-    getrs_interleaved_kernel<<<(unsigned)groups, 32, 0, s>>>(d, batch, info, offsets, workspace);
-    return check_launch();
-}
-
 int blastgpu_dgetrs_strided(int n, int nrhs, const double* LU, int lda, int64_t stride_a,
                             const int32_t* ipiv, int64_t stride_ipiv, double* X, int ldx,
                             int64_t stride_x, const int32_t* info, int64_t batch,
@@ -615,22 +534,23 @@ int blastgpu_dgetrs_strided(int n, int nrhs, const double* LU, int lda, int64_t 
     if (batch < 0) return -12;
     if (batch == 0 || n == 0 || nrhs == 0) return BLASTGPU_SUCCESS;
     StridedGetrs g{n, nrhs, lda, ldx, LU, stride_a, ipiv, stride_ipiv, X, stride_x};
-    return launch_getrs(g, batch, info, as_cuda(stream));
+    return launch_getrs(g, batch, n, info, as_cuda(stream));
 }
 
-int blastgpu_dgetrs_batched(const blastgpu_getrf_desc* desc, const int32_t* info, int64_t batch,
+int blastgpu_dgetrs_batched(const blastgpu_getrf_desc* desc, const int32_t* info, int64_t batch, int max_n,
                             blastgpu_stream_t stream) {
     if (batch < 0) return -3;
+    if (max_n < 0) return -4;
     if (batch == 0) return BLASTGPU_SUCCESS;
     if (!desc) return -1;
-    return launch_getrs(DescGetrs{desc}, batch, info, as_cuda(stream));
+    return launch_getrs(DescGetrs{desc}, batch, max_n, info, as_cuda(stream));
 }
 
 int blastgpu_dgesv_batched(const blastgpu_getrf_desc* desc, int32_t* info, int64_t batch,
                            int max_n, blastgpu_stream_t stream) {
     int st = blastgpu_dgetrf_batched(desc, info, batch, max_n, stream);
     if (st != BLASTGPU_SUCCESS) return st;
-    return blastgpu_dgetrs_batched(desc, info, batch, stream);
+    return blastgpu_dgetrs_batched(desc, info, batch, max_n, stream);
 }
 
 }  // extern "C"

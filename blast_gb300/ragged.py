@@ -184,16 +184,6 @@ class GesvPlan:
         big = int(np.sum(sorted_n > 64))
         self.bins = [(b0, b1, int(sorted_n[b0])) for b0, b1 in ((0, big), (big, self.count)) if b1 > b0]
         self.side = torch.cuda.Stream(device)
-        # getrs through a lane-interleaved copy of the factors (groups of 32 sorted instances)
-        ns = np.ascontiguousarray(sorted_n, dtype=np.int32)
-        rs = np.ascontiguousarray(B.cols[self.order], dtype=np.int32)
-        offs = np.zeros((self.count + 31) // 32 + 1, dtype=np.int64)
-        nbytes = _lib.lib().blastgpu_dgetrs_interleave_plan(ns.ctypes.data, rs.ctypes.data, self.count,
-                                                            offs.ctypes.data)
-        if nbytes < 0:
-            raise ValueError("invalid sizes")
-        self.offsets = torch.from_numpy(offs).to(device)
-        self.workspace = torch.empty(max(1, nbytes // 8), dtype=torch.float64, device=device)
 
     def _getrf(self, b0, b1, max_n, s):
         _lib.call("blastgpu_dgetrf_batched", self.d.data_ptr() + b0 * desc.GETRF_DTYPE.itemsize,
@@ -213,8 +203,8 @@ class GesvPlan:
             done = torch.cuda.Event()
             done.record(self.side)
             cur.wait_event(done)
-        _lib.call("blastgpu_dgetrs_batched_ws", self.d.data_ptr(), self.info.data_ptr(), self.count,
-                  self.offsets.data_ptr(), self.workspace.data_ptr(), cur.cuda_stream)
+        _lib.call("blastgpu_dgetrs_batched", self.d.data_ptr(), self.info.data_ptr(), self.count,
+                  self.bins[0][2], cur.cuda_stream)
 
     def capture(self):
         """Records run() into a CUDA graph; returns the torch.cuda.CUDAGraph (call .replay())."""

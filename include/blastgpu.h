@@ -280,18 +280,10 @@ typedef struct blastgpu_getrf_desc {
  * sizes, one CTA per matrix above n = 64 (tunable per size bin). */
 int blastgpu_dgetrf_batched(const blastgpu_getrf_desc* desc, int32_t* info, int64_t batch,
                             int max_n, blastgpu_stream_t stream);
-int blastgpu_dgetrs_batched(const blastgpu_getrf_desc* desc, const int32_t* info, int64_t batch,
+/* getrs on every instance (BLAST's laswp + trsm<Lower, unit> + trsm<Upper> order); max_n bounds
+ * every n (at most 800). Instances with info != 0 are skipped. */
+int blastgpu_dgetrs_batched(const blastgpu_getrf_desc* desc, const int32_t* info, int64_t batch, int max_n,
                             blastgpu_stream_t stream);
-/* getrs through a lane-interleaved copy of the factors: the same results bit for bit, with
- * coalesced loads (faster for ragged batches of larger n). Instances are taken in groups of 32
- * consecutive descriptors; blastgpu_dgetrs_interleave_plan fills offsets[0..ceil(batch/32)] (host
- * memory, in doubles) from the host arrays n[b] and nrhs[b] and returns the workspace size in
- * bytes (or -1 for invalid sizes); copy offsets to device memory and pass a device workspace of
- * that size. No reference counterpart (BLAST has no getrs; the composition follows
- * dense/Laswp.hpp:37-43 and dense/Trsm.hpp:39-65). */
-int64_t blastgpu_dgetrs_interleave_plan(const int32_t* n, const int32_t* nrhs, int64_t batch, int64_t* offsets);
-int blastgpu_dgetrs_batched_ws(const blastgpu_getrf_desc* desc, const int32_t* info, int64_t batch,
-                               const int64_t* offsets, double* workspace, blastgpu_stream_t stream);
 /* getrf followed by getrs on every instance (two launches on `stream`). */
 int blastgpu_dgesv_batched(const blastgpu_getrf_desc* desc, int32_t* info, int64_t batch,
                            int max_n, blastgpu_stream_t stream);

@@ -134,9 +134,9 @@ def test_gesv_ragged_log_uniform(gpu, oracle_lib):
         assert np.array_equal(dB.cpu().numpy(), xr), n
 
 
-def test_getrs_interleaved_matches_oracle(gpu, oracle_lib):
-    """blastgpu_dgetrs_batched_ws (lane-interleaved copy of the factors): unsorted ragged sizes,
-    several right-hand sides, groups that end part-way; bit-identical to the oracle's getrs."""
+def test_getrs_batched_ragged_matches_oracle(gpu, oracle_lib):
+    """blastgpu_dgetrs_batched on unsorted ragged sizes with several right-hand sides and a
+    partial last warp; bit-identical to the oracle's getrs."""
     import torch
 
     from blast_gb300 import _lib, desc
@@ -156,25 +156,20 @@ def test_getrs_interleaved_matches_oracle(gpu, oracle_lib):
         recs[i] = (desc.mat_record(dA), p.data_ptr(), desc.mat_record(dB))
         keep.append((LUr, pr, dB, p, dA))
     d = desc.upload(recs, "cuda")
-    n32, r32 = ns.astype(np.int32), rs.astype(np.int32)
-    offs = np.zeros((count + 31) // 32 + 1, dtype=np.int64)
-    nbytes = _lib.lib().blastgpu_dgetrs_interleave_plan(n32.ctypes.data, r32.ctypes.data, count, offs.ctypes.data)
-    assert nbytes == offs[-1] * 8 > 0
-    dOffs = torch.from_numpy(offs).cuda()
-    ws = torch.full((nbytes // 8,), float("nan"), dtype=torch.float64, device="cuda")
     info = torch.zeros(count, dtype=torch.int32, device="cuda")
-    _lib.call("blastgpu_dgetrs_batched_ws", d.data_ptr(), info.data_ptr(), count, dOffs.data_ptr(),
-              ws.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    _lib.call("blastgpu_dgetrs_batched", d.data_ptr(), info.data_ptr(), count, int(ns.max()),
+              torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
     for (LUr, pr, dB, p, dA), B in zip(keep, Bs):
         Xr = np.asfortranarray(B.copy())
         oracle_lib.getrs(LUr, pr, Xr, Xr)
         assert np.array_equal(dB.cpu().numpy(), Xr)
-    assert _lib.lib().blastgpu_dgetrs_interleave_plan(n32.ctypes.data, r32.ctypes.data, -1, None) == -1
+    assert _lib.lib().blastgpu_dgetrs_batched(d.data_ptr(), info.data_ptr(), count, -1, None) == -4
+    assert _lib.lib().blastgpu_dgetrs_batched(d.data_ptr(), info.data_ptr(), count, 801, None) == -1004
 
 
 def test_gesv_plan_log_uniform(gpu, oracle_lib):
-    """GesvPlan (two getrf bins on forked streams, then the interleaved getrs) on the ragged LU
+    """GesvPlan (two getrf bins on forked streams, then getrs) on the ragged LU
     workload's size distribution: pivots and solutions bit-identical to the oracle."""
     import torch
 
