@@ -339,12 +339,14 @@ struct DescGetrs {
 // getrs, one thread per instance, in BLAST's scalar order (dense/Trsm.hpp:39-65): laswp(b) with
 // ipiv[0..n), x_i = b_i - sum_{k<i} l_ik x_k (unit lower), x_i = (x_i - sum_{k>i} u_ik x_k) / u_ii,
 // every sum in ascending k. The solution vector lives in shared memory (x[k * 32 + lane], max_n * 32
-// doubles per warp). A dependent binary64 FMA chain is latency-bound on GB300, so the forward solve
-// runs four rows' chains side by side (each still in ascending k); the backward chain is inherently
-// serial in BLAST's order (row i starts from x_{i+1}). Factor terms are loaded a pass ahead of the
-// FMAs that use them (forward: 4 rows x 8 terms; backward: 16 terms along the row, the next row's
-// first pass and diagonal included), so memory latency overlaps the chain. A short pass reads
-// zeros past the row's end and skips their FMAs.
+// doubles per warp). The forward solve runs four rows' chains side by side (each still in ascending
+// k), so every x_k read serves four rows and a pass keeps 32 factor loads in flight; the backward
+// chain is serial in BLAST's order (row i starts from x_{i+1}). Factor terms are loaded a pass
+// ahead of the FMAs that use them (forward: 4 rows x 8 terms; backward: 16 terms along the row,
+// the next row's first pass and diagonal included), so memory latency overlaps the chain. On
+// GB300 a warp's DFMA occupies its sub-partition's binary64 pipe for 64 cycles, so the largest
+// instances' n^2 chained FMAs bound the kernel. A short pass reads zeros past the row's end and
+// skips their FMAs.
 struct FactorView {
     const double* p;
     int64_t ld;
