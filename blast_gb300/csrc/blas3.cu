@@ -37,6 +37,8 @@ struct Strided {
     }
 };
 
+// ALPHA1: alpha is 1, so alpha*a is a exactly and the multiplication is left out (same bits).
+template <bool ALPHA1>
 __global__ void __launch_bounds__(128) syrk_lower_kernel(int m, int k, double alpha, Strided A, double beta,
                                                          Strided C, Strided D, int64_t batch) {
     int64_t const b = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5);
@@ -49,7 +51,7 @@ __global__ void __launch_bounds__(128) syrk_lower_kernel(int m, int k, double al
         while (rem >= m - j) { rem -= m - j; ++j; }
         int const i = j + rem;
         double v = beta * C.at(b, i, j);
-        for (int q = 0; q < k; ++q) v = fma(alpha * A.at(b, i, q), A.at(b, j, q), v);
+        for (int q = 0; q < k; ++q) v = fma(ALPHA1 ? A.at(b, i, q) : alpha * A.at(b, i, q), A.at(b, j, q), v);
         D.at(b, i, j) = v;
     }
 }
@@ -76,6 +78,7 @@ __global__ void __launch_bounds__(128) trsm_kernel(int uplo, int trans_a, int un
     }
 }
 
+template <bool ALPHA1>
 __global__ void __launch_bounds__(128) trmm_kernel(int side, int uplo, int unit, int m, int n, double alpha,
                                                    Strided A, Strided B, Strided C, int64_t batch) {
     int64_t const b = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5);
@@ -88,10 +91,10 @@ __global__ void __launch_bounds__(128) trmm_kernel(int side, int uplo, int unit,
         double acc = 0.0;
         if (side == BLASTGPU_LEFT) {
             int const q0 = upper ? i : 0, q1 = upper ? m : i + 1;
-            for (int q = q0; q < q1; ++q) acc = fma(alpha * a(i, q), B.at(b, q, j), acc);
+            for (int q = q0; q < q1; ++q) acc = fma(ALPHA1 ? a(i, q) : alpha * a(i, q), B.at(b, q, j), acc);
         } else {
             int const q0 = upper ? 0 : j, q1 = upper ? j + 1 : n;
-            for (int q = q0; q < q1; ++q) acc = fma(alpha * B.at(b, i, q), a(q, j), acc);
+            for (int q = q0; q < q1; ++q) acc = fma(ALPHA1 ? B.at(b, i, q) : alpha * B.at(b, i, q), a(q, j), acc);
         }
         C.at(b, i, j) = acc;
     }
@@ -134,7 +137,10 @@ int launch_syrk_lower(int m, int k, int trans_a, double alpha, const double* A, 
     Strided a{const_cast<double*>(A), lda, sa, trans_a ? BLASTGPU_ROW_MAJOR : BLASTGPU_COL_MAJOR};
     Strided c{const_cast<double*>(C), ldc, sc, BLASTGPU_COL_MAJOR};
     Strided d{D, ldd, sd, BLASTGPU_COL_MAJOR};
-    syrk_lower_kernel<<<(unsigned)((batch + 3) / 4), 128, 0, s>>>(m, k, alpha, a, beta, c, d, batch);
+    if (alpha == 1.0)
+        syrk_lower_kernel<true><<<(unsigned)((batch + 3) / 4), 128, 0, s>>>(m, k, alpha, a, beta, c, d, batch);
+    else
+        syrk_lower_kernel<false><<<(unsigned)((batch + 3) / 4), 128, 0, s>>>(m, k, alpha, a, beta, c, d, batch);
     return check_launch();
 }
 
@@ -206,8 +212,11 @@ int blastgpu_dtrmm_strided(int side, int uplo, int unit, int m, int n, double al
     Strided a{const_cast<double*>(A), lda, stride_a, BLASTGPU_COL_MAJOR};
     Strided bb{const_cast<double*>(B), ldb, stride_b, BLASTGPU_COL_MAJOR};
     Strided c{C, ldc, stride_c, BLASTGPU_COL_MAJOR};
-    trmm_kernel<<<(unsigned)((batch + 3) / 4), 128, 0, as_cuda(stream)>>>(side, uplo, unit, m, n, alpha, a, bb, c,
-                                                                         batch);
+    unsigned const blocks = (unsigned)((batch + 3) / 4);
+    if (alpha == 1.0)
+        trmm_kernel<true><<<blocks, 128, 0, as_cuda(stream)>>>(side, uplo, unit, m, n, alpha, a, bb, c, batch);
+    else
+        trmm_kernel<false><<<blocks, 128, 0, as_cuda(stream)>>>(side, uplo, unit, m, n, alpha, a, bb, c, batch);
     return check_launch();
 }
 

@@ -59,7 +59,9 @@ struct LoadSrc {
 // SyrkSrc: beta*C + alpha*A*A^T (A: n x K, or K x n read transposed), formed tile by tile in the
 // order of blast::syrkLower (dense/Syrk.hpp:15-145): v = beta*c_ij rounded (RegisterMatrix::load(
 // beta, ..)), then for l ascending v = fma(alpha*a_il, a_jl, v) (RegisterMatrix::ger(alpha, ..)).
-// The factorisation then runs on exactly the values syrkLower would have stored.
+// The factorisation then runs on exactly the values syrkLower would have stored. ALPHA1: alpha is
+// 1, so alpha*a_il is a_il exactly and its multiplication is left out.
+template <bool ALPHA1>
 struct SyrkSrc {
     const double* A;
     int64_t lda;
@@ -82,7 +84,7 @@ struct SyrkSrc {
         for (int l = 0; l < K; ++l) {
             double ax[KM], b[KN];
 #pragma unroll
-            for (int r = 0; r < KM; ++r) ax[r] = (i + r < n) ? alpha * a(i + r, l) : 0.0;
+            for (int r = 0; r < KM; ++r) ax[r] = (i + r < n) ? (ALPHA1 ? a(i + r, l) : alpha * a(i + r, l)) : 0.0;
 #pragma unroll
             for (int c = 0; c < KN; ++c) b[c] = (c < nc) ? a(k + c, l) : 0.0;
 #pragma unroll
@@ -441,10 +443,11 @@ struct SyrkPotrfArgs {
     int64_t batch;
 };
 
+template <bool ALPHA1>
 __global__ void __launch_bounds__(32, 12) syrk_potrf_thread_kernel(SyrkPotrfArgs p) {
     int64_t const b = (int64_t)blockIdx.x * 32 + threadIdx.x;
     if (b >= p.batch) return;
-    SyrkSrc const src{p.A + b * p.sa, p.lda, p.k, p.trans != 0, p.alpha, p.beta, p.C + b * p.sc, p.ldc};
+    SyrkSrc<ALPHA1> const src{p.A + b * p.sa, p.lda, p.k, p.trans != 0, p.alpha, p.beta, p.C + b * p.sc, p.ldc};
     int const info = potrf_thread_src<4, 4>(p.n, src, p.D + b * p.sd, ColAddr{p.ldd});
     if (p.info) p.info[b] = info;
 }
@@ -608,11 +611,14 @@ int blastgpu_dsyrk_potrf_strided(int n, int k, int trans_a, double alpha, const 
         }
         return BLASTGPU_SUCCESS;
     }
-    // The fused kernel runs one thread per instance; below a few warps per SM its serial syrk part
-    // is exposed, and syrkLower's warp-per-instance kernel followed by the thread-per-matrix potrf
-    // is faster (measured on GB300: 4.4 ms vs 7.0 ms at 10,000 instances of n = 60, k = 30; 14.8
-    // vs 11.8 ms at 50,000). Both give the same bits.
-    if (batch < tune_get("syrk_potrf.fused_min_batch", sm_count() * 192)) {
+    // Two implementations with the same bits: syrkLower's warp-per-instance kernel followed by the
+    // thread-per-matrix potrf, or the fused thread-per-matrix kernel, which never stores the sum
+    // but runs the syrk part at thread-per-matrix granularity (1,563 warps for 50,000 instances,
+    // unevenly spread over the 608 sub-partitions). Measured on GB300 at n = 60, k = 30, alpha = 1:
+    // 8.85 ms for the pair vs 9.42 ms fused at 50,000 instances, and the pair is further ahead at
+    // smaller batches, so the pair is the default; "syrk_potrf.fused_min_batch" selects the fused
+    // kernel from that batch size on.
+    if (batch < tune_get("syrk_potrf.fused_min_batch", 0x7fffffff)) {
         int st = launch_syrk_lower(n, k, trans_a, alpha, A, lda, stride_a, beta, C, ldc, stride_c, D, ldd,
                                    stride_d, batch, s);
         if (st != BLASTGPU_SUCCESS) return st;
@@ -623,7 +629,10 @@ int blastgpu_dsyrk_potrf_strided(int n, int k, int trans_a, double alpha, const 
     if (blocks > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
     SyrkPotrfArgs const p{n, k, trans_a, alpha, beta, A, lda, stride_a, C, ldc, stride_c, D, ldd, stride_d, info,
                           batch};
-    syrk_potrf_thread_kernel<<<(unsigned)blocks, 32, 0, s>>>(p);
+    if (alpha == 1.0)
+        syrk_potrf_thread_kernel<true><<<(unsigned)blocks, 32, 0, s>>>(p);
+    else
+        syrk_potrf_thread_kernel<false><<<(unsigned)blocks, 32, 0, s>>>(p);
     return check_launch();
 }
 

@@ -22,7 +22,7 @@ def test_syrk_lower_sweep_bitexact(gpu, oracle_lib):
             A = rng.random((batch, m, k))
             C = rng.random((batch, m, m))
             C = C + np.swapaxes(C, 1, 2)
-            alpha, beta = 0.75, -1.25
+            alpha, beta = (1.0 if k % 2 == 0 else 0.75), -1.25  # alpha = 1 takes its own code path
             dA, dC = to_dev(A), to_dev(C)
             dD = to_dev(np.full((batch, m, m), 3.0))
             gpu.syrk_lower(alpha, dA, beta, dC, dD)
@@ -120,7 +120,7 @@ def test_trmm_variants_blast_leaves_out(gpu, oracle_lib, side, uplo, unit):
             k = m if side == 0 else n
             A = rng.random((batch, k, k))
             B = rng.random((batch, m, n))
-            alpha = 0.625
+            alpha = 1.0 if n % 2 == 0 else 0.625
             dA, dB = to_dev(A), to_dev(B)
             dC = gpu.col_major((batch,), m, n, "cuda")
             if side == 0:

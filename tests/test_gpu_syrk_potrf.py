@@ -16,18 +16,14 @@ def F(a):
 
 @pytest.fixture(params=["fused", "two_launch"])
 def path(request, gpu):
-    """Both code paths of blastgpu_dsyrk_potrf_strided: the fused kernel (large batches) and
-    syrkLower then potrf (small batches), forced through the tuning key that separates them."""
+    """Both code paths of blastgpu_dsyrk_potrf_strided: the fused kernel and syrkLower then potrf
+    (the default), forced through the tuning key that separates them."""
     from blast_gb300 import _lib
 
     old = _lib.tune_get("syrk_potrf.fused_min_batch")
     _lib.tune_set("syrk_potrf.fused_min_batch", 0 if request.param == "fused" else 1 << 30)
     yield request.param
-    if old is None:  # the library's default: 192 instances per SM
-        import torch
-
-        old = torch.cuda.get_device_properties(0).multi_processor_count * 192
-    _lib.tune_set("syrk_potrf.fused_min_batch", old)
+    _lib.tune_set("syrk_potrf.fused_min_batch", old if old is not None else 0x7FFFFFFF)  # default: pair
 
 
 def _case(rng, batch, n, k):
@@ -46,7 +42,7 @@ def test_syrk_potrf_matches_composition(gpu, oracle_lib, trans, path):
     for n, k in shapes:
         batch = 6
         A, C = _case(rng, batch, n, k)
-        alpha, beta = 0.75, 1.0 if k % 2 else 0.5
+        alpha, beta = (1.0 if n % 2 else 0.75), (1.0 if k % 2 else 0.5)  # alpha = 1: own code path
         # op(A) = A (n x k, column-major) or the row-major view of a k x n column-major matrix
         dA = to_dev(np.swapaxes(A, 1, 2)).mT if trans else to_dev(A)
         dC = to_dev(C)
