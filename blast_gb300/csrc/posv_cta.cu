@@ -291,102 +291,99 @@ __device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf,
     return *s_info;
 }
 
-// Stages the nb x nb diagonal block at (j0, j0) of F into blk (column-major, stride 33), with
-// an identity completion outside nb.
+// In-place solve with the factor: v := F^{-T} F^{-1} v (v in shared memory, precision T).
+// Blockwise with look-ahead, one barrier per 32-row block: once block b is solved, warp 0 applies
+// it to the next block's 32 entries and solves that block's 32 x 32 triangle from registers
+// (loaded straight from the factor, shuffles along the chain), while warps 1..7 apply block b to
+// all entries beyond. Forward: row i of v takes each block's columns in order, j ascending;
+// backward: entry i takes each solved block's rows r ascending, blocks from the bottom.
 template <typename T>
-__device__ __forceinline__ void stage_block(const T* F, int ldf, int j0, int nb, T* blk) {
-    for (int idx = threadIdx.x; idx < 32 * 32; idx += kThreads) {
-        int const r = idx & 31, c = idx >> 5;
-        if (r < nb && c < nb) cp_async(blk + c * 33 + r, F + (j0 + r) + (int64_t)(j0 + c) * ldf);
-        else blk[c * 33 + r] = (T)(r == c ? 1 : 0);
+__device__ __forceinline__ void potrs_fwd_block(const T* F, int ldf, int n, int j0, T* v, int lane) {
+    int const nb = min(32, n - j0);
+    T a[32];
+#pragma unroll
+    for (int k = 0; k < 32; ++k)
+        a[k] = (lane < nb && k < lane) ? F[(j0 + lane) + (int64_t)(j0 + k) * ldf] : (T)0;
+    T const rd = rcp_t<T>(lane < nb ? F[(j0 + lane) + (int64_t)(j0 + lane) * ldf] : (T)1);
+    T x = lane < nb ? v[j0 + lane] : (T)0;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        if (lane == j) x *= rd;
+        T const xj = __shfl_sync(0xffffffffu, x, j);
+        if (lane > j) x = fma(-a[j], xj, x);
     }
-    cp_async_wait_all();
+    if (lane < nb) v[j0 + lane] = x;
 }
 
-// In-place solve with the factor: v := F^{-T} F^{-1} v (v in shared memory, precision T).
-// Each 32 x 32 diagonal block is solved by one warp from registers (rows for the forward pass,
-// columns for the backward pass), fully unrolled; the other rows are updated by all threads.
+template <typename T>
+__device__ __forceinline__ void potrs_bwd_block(const T* F, int ldf, int n, int j0, T* v, int lane) {
+    int const nb = min(32, n - j0);
+    T c[32];  // column lane of the block: c[k] = F(j0 + k, j0 + lane), k > lane
+#pragma unroll
+    for (int k = 0; k < 32; ++k)
+        c[k] = (lane < nb && k > lane && k < nb) ? F[(j0 + k) + (int64_t)(j0 + lane) * ldf] : (T)0;
+    T const rd = rcp_t<T>(lane < nb ? F[(j0 + lane) + (int64_t)(j0 + lane) * ldf] : (T)1);
+    T x = lane < nb ? v[j0 + lane] : (T)0;
+#pragma unroll
+    for (int j = 31; j >= 0; --j) {
+        if (lane == j) x *= rd;
+        T const xj = __shfl_sync(0xffffffffu, x, j);
+        if (lane < j) x = fma(-c[j], xj, x);
+    }
+    if (lane < nb) v[j0 + lane] = x;
+}
+
 template <typename T, int MAXR>
-__device__ void cta_potrs(int n, const T* F, int ldf, T* v, T* blk) {
-    __shared__ T red[kWarps * 32];
+__device__ void cta_potrs(int n, const T* F, int ldf, T* v, T* /*blk*/) {
     int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    int const nblk = (n + 31) / 32;
     // forward: F * y = v
-    for (int j0 = 0; j0 < n; j0 += 32) {
-        int const nb = min(32, n - j0);
-        stage_block<T>(F, ldf, j0, nb, blk);
-        __syncthreads();
+    if (warp == 0) potrs_fwd_block<T>(F, ldf, n, 0, v, lane);
+    __syncthreads();
+    for (int b = 0; b + 1 < nblk; ++b) {
+        int const j0 = 32 * b, jn = j0 + 32, nbn = min(32, n - jn);  // block b is 32 wide
         if (warp == 0) {
-            T a[32];
+            if (lane < nbn) {
+                int const r = jn + lane;
+                T acc = v[r];
 #pragma unroll
-            for (int k = 0; k < 32; ++k) a[k] = blk[k * 33 + lane];
-            T const rd = rcp_t<T>(blk[lane * 33 + lane]);
-            T x = lane < nb ? v[j0 + lane] : (T)0;
-#pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                if (lane == j) x *= rd;
-                T const xj = __shfl_sync(0xffffffffu, x, j);
-                if (lane > j) x = fma(-a[j], xj, x);
+                for (int j = 0; j < 32; ++j) acc = fma(-F[r + (int64_t)(j0 + j) * ldf], v[j0 + j], acc);
+                v[r] = acc;
             }
-            if (lane < nb) v[j0 + lane] = x;
-        }
-        __syncthreads();
-        for (int r = j0 + nb + tid; r < n; r += kThreads) {
-            T acc = v[r];
+            __syncwarp();
+            potrs_fwd_block<T>(F, ldf, n, jn, v, lane);
+        } else {
+            for (int r = jn + 32 + (tid - 32); r < n; r += kThreads - 32) {
+                T acc = v[r];
 #pragma unroll
-            for (int j = 0; j < 32; ++j)
-                if (j < nb) acc = fma(-F[r + (int64_t)(j0 + j) * ldf], v[j0 + j], acc);
-            v[r] = acc;
+                for (int j = 0; j < 32; ++j) acc = fma(-F[r + (int64_t)(j0 + j) * ldf], v[j0 + j], acc);
+                v[r] = acc;
+            }
         }
         __syncthreads();
     }
     // backward: F^T * x = y, blocks from the bottom
-    int const last = ((n - 1) / 32) * 32;
-    for (int j0 = last; j0 >= 0; j0 -= 32) {
-        int const nb = min(32, n - j0);
-        // rows of this block take the contributions of the rows below: v_i -= sum_r F(r,i) v_r.
-        // Every thread takes rows r = j0+nb+tid, +256, ... and accumulates all 32 columns (loads
-        // coalesced across threads for each column, all independent); the 8 warps' partial sums
-        // are then reduced through shared memory (red: 8 x 32 values).
-        if (j0 + nb < n) {
-            T part[32];
-#pragma unroll
-            for (int i = 0; i < 32; ++i) part[i] = (T)0;
-            for (int r = j0 + nb + tid; r < n; r += kThreads) {
-                T const vr = v[r];
-                T const* row = F + r + (int64_t)j0 * ldf;
-#pragma unroll
-                for (int i = 0; i < 32; ++i)
-                    if (i < nb) part[i] = fma(row[(int64_t)i * ldf], vr, part[i]);
-            }
-#pragma unroll
-            for (int i = 0; i < 32; ++i) {
-                T x = part[i];
-#pragma unroll
-                for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
-                if (lane == i) red[warp * 32 + i] = x;
-            }
-            __syncthreads();
-            if (tid < nb) {
-                T acc = (T)0;
-                for (int w = 0; w < kWarps; ++w) acc += red[w * 32 + tid];
-                v[j0 + tid] -= acc;
-            }
-        }
-        stage_block<T>(F, ldf, j0, nb, blk);
-        __syncthreads();
+    if (warp == 0) potrs_bwd_block<T>(F, ldf, n, 32 * (nblk - 1), v, lane);
+    __syncthreads();
+    for (int b = nblk - 1; b > 0; --b) {
+        int const j0 = 32 * b, jp = j0 - 32, nb = min(32, n - j0);  // block b - 1 is 32 wide
         if (warp == 0) {
-            T c[32];
-#pragma unroll
-            for (int k = 0; k < 32; ++k) c[k] = blk[lane * 33 + k];  // column lane: F(k, lane)
-            T const rd = rcp_t<T>(blk[lane * 33 + lane]);
-            T x = lane < nb ? v[j0 + lane] : (T)0;
-#pragma unroll
-            for (int j = 31; j >= 0; --j) {
-                if (lane == j) x *= rd;
-                T const xj = __shfl_sync(0xffffffffu, x, j);
-                if (lane < j) x = fma(-c[j], xj, x);
+            int const i = jp + lane;
+            T acc = v[i];
+            const T* col = F + j0 + (int64_t)i * ldf;
+#pragma unroll 8
+            for (int r = 0; r < nb; ++r) acc = fma(-col[r], v[j0 + r], acc);
+            v[i] = acc;
+            __syncwarp();
+            potrs_bwd_block<T>(F, ldf, n, jp, v, lane);
+        } else {
+            for (int i = tid - 32; i < jp; i += kThreads - 32) {
+                T acc = v[i];
+                const T* col = F + j0 + (int64_t)i * ldf;
+#pragma unroll 8
+                for (int r = 0; r < nb; ++r) acc = fma(-col[r], v[j0 + r], acc);
+                v[i] = acc;
             }
-            if (lane < nb) v[j0 + lane] = x;
         }
         __syncthreads();
     }
