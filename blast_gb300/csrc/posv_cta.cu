@@ -153,16 +153,18 @@ __device__ __forceinline__ void panel_update_dispatch(T (&acc)[MAXR][4], const T
 }
 
 // Cholesky of the nb x nb diagonal block held in shared memory (column j at blk + j * NMAX),
-// right-looking, all threads. Column j is final (scaled) before step j: step j updates the
-// trailing block a_il = fma(-l_ij, l_lj, a_il) (warp w: columns l = j+1+w, j+1+w+8, ...; lane: row
-// l + lane), and warp 0, which owns column j+1, finishes it in the same step: the new pivot
+// column at a time, all threads (used for binary64, where warp 0's dependent reciprocal square
+// roots cost 64 cycles per step and the sub-panel version below is slower). Column j is final
+// (scaled) before step j: step j updates the trailing block a_il = fma(-l_ij, l_lj, a_il) (warp w:
+// columns l = j+1+w, j+1+w+8, ...; lane: row l + lane), and warp 0, which owns column j+1,
+// finishes it in the same step: the new pivot
 // d = a_{j+1,j+1} comes from lane 0 by a shuffle, y = 1/sqrt(d), and the column is stored as
 // a_{i,j+1} * y. Every element is then a single fused multiply-add per step, the reciprocal
 // square root is taken by one warp, and there is one barrier per column. The products equal
 // RegisterMatrix::potrf's (the pivot column scaled by 1/sqrt(d) once, then used unrounded).
 // rinv[j] = 1/l_jj. Records the first bad pivot (k0 + j + 1) in *s_info.
 template <typename T, int NMAX>
-__device__ __forceinline__ void cta_chol_block(T* blk, int nb, int k0, T* rinv, int* s_info) {
+__device__ __forceinline__ void cta_chol_block_cols(T* blk, int nb, int k0, T* rinv, int* s_info) {
     int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (warp == 0) {
         T const v = lane < nb ? blk[lane] : (T)0;
@@ -190,6 +192,70 @@ __device__ __forceinline__ void cta_chol_block(T* blk, int nb, int k0, T* rinv, 
                 if (i < nb) blk[l * NMAX + i] = v * y;
             } else if (i < nb) {
                 blk[l * NMAX + i] = v;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Cholesky of the nb x nb diagonal block held in shared memory (column j at blk + j * NMAX),
+// right-looking in sub-panels of 8 columns. Warp 0 (lane = row of the block) factors a sub-panel
+// in registers: pivot d from the owning lane by a shuffle, y = 1/sqrt(d), l_jj = d*y, l_ij = a_ij*y,
+// then the sub-panel's later columns take fma(-l_ij, l_lj, .) with l_lj shuffled from lane l. All
+// threads then apply the 8 columns to the rest of the block, element by element in column order.
+// Every element sees the same fused multiply-adds in the same order as the column-at-a-time
+// version above (RegisterMatrix::potrf's products), with 2 barriers per 8 columns; binary32 only.
+// rinv[j] = 1/l_jj. Records the first bad pivot (k0 + j + 1) in *s_info.
+template <typename T, int NMAX>
+__device__ __forceinline__ void cta_chol_block(T* blk, int nb, int k0, T* rinv, int* s_info) {
+    if constexpr (sizeof(T) == 8) {
+        cta_chol_block_cols<T, NMAX>(blk, nb, k0, rinv, s_info);
+        return;
+    }
+    int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int s0 = 0; s0 < nb; s0 += 8) {
+        int const ns = min(8, nb - s0);
+        if (warp == 0) {
+            int const i = lane;  // row of the block
+            T v[8];
+#pragma unroll
+            for (int c = 0; c < 8; ++c) v[c] = (c < ns && i >= s0 + c && i < nb) ? blk[(s0 + c) * NMAX + i] : (T)0;
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                if (c < ns) {  // warp-uniform
+                    int const j = s0 + c;
+                    T const d = __shfl_sync(0xffffffffu, v[c], j);
+                    T const y = rsqrt_t<T>(d);
+                    if (lane == 0) {
+                        if (!(d > (T)0) && *s_info == 0) *s_info = k0 + j + 1;
+                        rinv[j] = y;
+                    }
+                    if (i == j) v[c] = d * y;
+                    else if (i > j) v[c] *= y;
+#pragma unroll
+                    for (int c2 = c + 1; c2 < 8; ++c2) {
+                        T const llj = __shfl_sync(0xffffffffu, v[c], s0 + c2);
+                        if (c2 < ns && i >= s0 + c2) v[c2] = fma(-v[c], llj, v[c2]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+                if (c < ns && i >= s0 + c && i < nb) blk[(s0 + c) * NMAX + i] = v[c];
+        }
+        __syncthreads();
+        // the block's columns l >= s0 + 8 take the sub-panel: a_il -= sum_c l_i,s0+c * l_l,s0+c
+        int const l0 = s0 + 8;
+        if (l0 < nb) {
+            int const w = nb - l0;  // columns l0 .. nb-1; element (i, l), i >= l
+            for (int e = tid; e < w * 32; e += kThreads) {
+                int const l = l0 + e / 32, i = l + (e & 31);
+                if (i < nb) {
+                    T acc = blk[l * NMAX + i];
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) acc = fma(-blk[(s0 + c) * NMAX + i], blk[(s0 + c) * NMAX + l], acc);
+                    blk[l * NMAX + i] = acc;
+                }
             }
         }
         __syncthreads();
