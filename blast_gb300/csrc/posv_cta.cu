@@ -315,6 +315,14 @@ __device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf,
                 rowsum[k0 + r] += t;
             }
         }
+        // The next panel's columns of A (lower part) start towards L2 while this panel is updated.
+        if (k0 + kNB < n) {
+            int const kn = k0 + kNB, cols = min(kNB, n - kn), lines = (n - kn + 15) / 16;
+            for (int e = tid; e < cols * lines; e += kThreads) {
+                int const c = e / lines, r = kn + (e - c * lines) * 16;
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(A + r + (int64_t)(kn + c) * lda));
+            }
+        }
         // Panel update with the previous columns.
         panel_update_dispatch<T, MAXR>(acc, F, ldf, buf, k0, m, c0);
         __syncthreads();
