@@ -10,14 +10,16 @@
 //  * Factorisation, left-looking with panels of 32 columns. Warp w owns panel columns
 //    4w..4w+3, lane l owns rows l, l+32, ..., so each thread keeps an MAXR x 4 register tile
 //    (BLAST's RegisterMatrix, 32 times wider). The update of a panel with all previous columns
-//    streams those columns through shared memory 16 at a time; every thread then performs
-//    MAXR*4 fused multiply-adds per column with operands read conflict-free from shared memory
-//    (rows: consecutive lanes; panel columns: a warp-uniform broadcast).
-//  * The 32 x 32 diagonal block is factored in place in shared memory (right-looking, all
-//    threads), the rows below are solved against it (one thread per row), and the panel is
-//    written to the factor.
-//  * Forward and backward substitution run blockwise: a warp solves each 32 x 32 triangle with
-//    shuffles, then all threads apply the block to the remaining rows.
+//    streams those columns through shared memory 32 at a time; every thread then performs
+//    RA*4 fused multiply-adds per column (RA = 32-row blocks still below the diagonal, fixed at
+//    compile time per panel) with operands read conflict-free from shared memory (rows:
+//    consecutive lanes; panel columns: a warp-uniform broadcast).
+//  * The 32 x 32 diagonal block is factored in place in shared memory (all threads; binary32 in
+//    sub-panels of 8 columns finished by warp 0 in registers), the rows below are solved against
+//    it (one thread per row), and the panel is written to the factor.
+//  * Forward and backward substitution run blockwise with look-ahead: once a 32-row block is
+//    solved, warp 0 applies it to the next block and solves that block's triangle from registers
+//    with shuffles while the other warps apply it to everything beyond; one barrier per block.
 //  * Mixed precision: the factor is binary32 (in the caller's workspace); the residual
 //    r = b - A*x is computed in binary64 from A's lower triangle, the correction solve uses the
 //    binary32 factor on the scaled residual, and each matrix iterates until its normwise
@@ -95,9 +97,8 @@ struct Smem {
     static constexpr int kPanelElems = kNB * NMAX;
     static constexpr int kStageElems = kKC * NMAX;
     static constexpr int kBufElems = kPanelElems > kStageElems ? kPanelElems : kStageElems;
-    static constexpr int kBlkElems = 32 * 33;  // one padded 32 x 32 diagonal block
     static constexpr size_t kBytes =
-        sizeof(T) * (kBufElems + kBlkElems) + sizeof(double) * (4 * NMAX + 64);
+        sizeof(T) * kBufElems + sizeof(double) * (4 * NMAX + 64);
 };
 
 // Update of the panel's register tiles with all previous columns: acc -= F(k0:n, kk) * F(k0+c, kk)
@@ -408,7 +409,7 @@ __device__ __forceinline__ void potrs_bwd_block(const T* F, int ldf, int n, int 
 }
 
 template <typename T, int MAXR>
-__device__ void cta_potrs(int n, const T* F, int ldf, T* v, T* /*blk*/) {
+__device__ void cta_potrs(int n, const T* F, int ldf, T* v) {
     int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     int const nblk = (n + 31) / 32;
     // forward: F * y = v
@@ -587,8 +588,7 @@ __global__ void __launch_bounds__(kThreads, MAXR <= 8 ? 2 : 1) posv_cta_f64_kern
     using S = Smem<double, MAXR>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double* buf = reinterpret_cast<double*>(smem_raw);
-    double* blk = buf + S::kBufElems;
-    double* vec = blk + S::kBlkElems;
+    double* vec = buf + S::kBufElems;
     __shared__ int s_info;
     int64_t const b = blockIdx.x;
     if (b >= args.batch) return;
@@ -599,7 +599,7 @@ __global__ void __launch_bounds__(kThreads, MAXR <= 8 ? 2 : 1) posv_cta_f64_kern
     for (int c = 0; c < it.nrhs; ++c) {
         for (int i = threadIdx.x; i < n; i += kThreads) vec[i] = it.B[i + (int64_t)c * it.ldb];
         __syncthreads();
-        cta_potrs<double, MAXR>(n, it.L, it.ldl, vec, blk);
+        cta_potrs<double, MAXR>(n, it.L, it.ldl, vec);
         for (int i = threadIdx.x; i < n; i += kThreads) it.X[i + (int64_t)c * it.ldx] = vec[i];
         __syncthreads();
     }
@@ -612,8 +612,7 @@ __global__ void __launch_bounds__(kThreads, 2) posv_cta_mixed_kernel(Batch batch
     constexpr int NMAX = S::NMAX;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* buf = reinterpret_cast<float*>(smem_raw);
-    float* blk = buf + S::kBufElems;
-    double* x = reinterpret_cast<double*>(smem_raw + sizeof(float) * (S::kBufElems + S::kBlkElems));
+    double* x = reinterpret_cast<double*>(smem_raw + sizeof(float) * S::kBufElems);
     double* r = x + NMAX;
     double* bb = r + NMAX;
     float* w = reinterpret_cast<float*>(bb + NMAX);  // NMAX floats (fits in the 4th vector)
@@ -650,7 +649,7 @@ __global__ void __launch_bounds__(kThreads, 2) posv_cta_mixed_kernel(Batch batch
         // x0 = F^{-T} F^{-1} b in binary32
         for (int i = tid; i < n; i += kThreads) w[i] = (float)bb[i];
         __syncthreads();
-        if (info == 0) cta_potrs<float, MAXR>(n, F, n, w, blk);
+        if (info == 0) cta_potrs<float, MAXR>(n, F, n, w);
         for (int i = tid; i < n; i += kThreads) x[i] = info == 0 ? (double)w[i] : CUDART_NAN;
         __syncthreads();
         double be = CUDART_NAN;  // a failed binary32 factorisation leaves no solution to refine
@@ -674,7 +673,7 @@ __global__ void __launch_bounds__(kThreads, 2) posv_cta_mixed_kernel(Batch batch
             double const s = rm;
             for (int i = tid; i < n; i += kThreads) w[i] = (float)(r[i] / s);
             __syncthreads();
-            cta_potrs<float, MAXR>(n, F, n, w, blk);
+            cta_potrs<float, MAXR>(n, F, n, w);
             for (int i = tid; i < n; i += kThreads) x[i] += (double)w[i] * s;
             __syncthreads();
             ++it_count;
@@ -720,8 +719,7 @@ __global__ void __launch_bounds__(kThreads, MAXR <= 4 ? 2 : 1)
     using S = Smem<double, MAXR>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double* buf = reinterpret_cast<double*>(smem_raw);
-    double* blk = buf + S::kBufElems;
-    double* vec = blk + S::kBlkElems;
+    double* vec = buf + S::kBufElems;
     __shared__ int s_info;
     int64_t const b = blockIdx.x;
     if (b >= count) return;
@@ -737,7 +735,7 @@ __global__ void __launch_bounds__(kThreads, MAXR <= 4 ? 2 : 1)
     for (int c = 0; c < it.nrhs; ++c) {
         for (int i = tid; i < n; i += kThreads) vec[i] = it.G[i + (int64_t)c * it.ldg];
         __syncthreads();
-        cta_potrs<double, MAXR>(n, it.L, it.ldl, vec, blk);
+        cta_potrs<double, MAXR>(n, it.L, it.ldl, vec);
         for (int i = tid; i < n; i += kThreads) it.GB[i + (int64_t)c * it.ldgb] = vec[i];
         __syncthreads();
     }
