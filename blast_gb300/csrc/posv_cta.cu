@@ -480,95 +480,71 @@ __device__ __forceinline__ double cta_max(double v, double* red) {
     return r;
 }
 
-// y = A*x for symmetric A given by its lower triangle (binary64); x, y in shared memory.
-// Part 1, y_i = sum_{j<=i} A(i,j) x_j, gives each thread the row pair (p, n-1-p), whose lengths
-// add up to n+1, so all threads do the same work; consecutive threads read consecutive rows of
-// each column. Part 2, y_i += sum_{j>i} A(j,i) x_j, runs a warp down each column.
-__device__ void cta_symv_lower(int n, const double* A, int lda, const double* x, double* y) {
+// y = A*x for symmetric A given by its lower triangle (binary64); x, y in shared memory; part:
+// kWarps * NMAX doubles of shared scratch. One pass over the lower triangle: a warp takes a group
+// of 16 columns (groups g and ng-1-g together, so that the warps' shares are even), lanes over
+// rows, and every element a_ji (j >= i) feeds both the row sum of j (in the lane, then the warp's
+// row partials in part) and, below the diagonal, the column sum of i (16 accumulators per lane,
+// folded across the warp at the end of the group). Each element is read once and costs its two
+// FMAs; the cross-lane sums take 16 additions per 16 columns.
+template <int NMAX>
+__device__ void cta_symv_lower(int n, const double* A, int lda, const double* x, double* y, double* part) {
     int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int p = tid; p < (n + 1) / 2; p += kThreads) {
-        int const q = n - 1 - p;
-        double a0[4] = {0.0, 0.0, 0.0, 0.0}, a1[4] = {0.0, 0.0, 0.0, 0.0};
-        int j = 0;
-        for (; j + 7 <= p; j += 8) {  // 16 loads in flight per thread
-            double ap[8], aq[8];
+    double* mine = part + warp * NMAX;
+    for (int i = lane; i < n; i += 32) mine[i] = 0.0;
+    __syncwarp();
+    int const ng = (n + 15) / 16;
+    for (int t = warp; t < (ng + 1) / 2; t += kWarps) {
+        for (int h = 0; h < 2; ++h) {
+            int const g = h == 0 ? t : ng - 1 - t;
+            if (h == 1 && g == t) break;
+            int const i0 = 16 * g, gc = min(16, n - i0);
+            double p[16], xc[16];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                ap[u] = A[p + (int64_t)(j + u) * lda];
-                aq[u] = A[q + (int64_t)(j + u) * lda];
+            for (int c = 0; c < 16; ++c) {
+                p[c] = 0.0;
+                xc[c] = c < gc ? x[i0 + c] : 0.0;
             }
+            for (int jb = i0; jb < n; jb += 32) {
+                int const j = jb + lane;
+                double const xj = j < n ? x[j] : 0.0;
+                double a[16];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                a0[u & 3] = fma(ap[u], x[j + u], a0[u & 3]);
-                a1[u & 3] = fma(aq[u], x[j + u], a1[u & 3]);
+                for (int c = 0; c < 16; ++c)
+                    a[c] = (j < n && c < gc && j >= i0 + c) ? A[j + (int64_t)(i0 + c) * lda] : 0.0;
+                double r = 0.0;
+#pragma unroll
+                for (int c = 0; c < 16; ++c) {
+                    r = fma(a[c], xc[c], r);
+                    p[c] = fma(a[c], j > i0 + c ? xj : 0.0, p[c]);
+                }
+                if (j < n) mine[j] += r;
             }
-        }
-        for (; j + 3 <= p; j += 4) {
-            double ap[4], aq[4];
+            // fold p[c] across the 32 lanes: after the halving steps lane l holds column (l & 15)'s
+            // sum over one half-warp; one more exchange adds the other half
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                ap[u] = A[p + (int64_t)(j + u) * lda];
-                aq[u] = A[q + (int64_t)(j + u) * lda];
+            for (int w = 8; w >= 1; w >>= 1) {
+                bool const upper = (lane & w) != 0;
+#pragma unroll
+                for (int c = 0; c < w; ++c) {
+                    double const give = upper ? p[c] : p[c + w];
+                    double const keep = upper ? p[c + w] : p[c];
+                    p[c] = keep + __shfl_xor_sync(0xffffffffu, give, w);
+                }
             }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                a0[u] = fma(ap[u], x[j + u], a0[u]);
-                a1[u] = fma(aq[u], x[j + u], a1[u]);
-            }
+            double const colsum = p[0] + __shfl_xor_sync(0xffffffffu, p[0], 16);
+            __syncwarp();
+            int const ci = lane & 15;
+            if (lane < 16 && ci < gc) mine[i0 + ci] += colsum;
+            __syncwarp();
         }
-        for (; j <= p; ++j) {
-            a0[0] = fma(A[p + (int64_t)j * lda], x[j], a0[0]);
-            a1[0] = fma(A[q + (int64_t)j * lda], x[j], a1[0]);
-        }
-        for (; j + 15 <= q; j += 16) {  // the long row alone: 16 loads in flight
-            double aq[16];
-#pragma unroll
-            for (int u = 0; u < 16; ++u) aq[u] = A[q + (int64_t)(j + u) * lda];
-#pragma unroll
-            for (int u = 0; u < 16; ++u) a1[u & 3] = fma(aq[u], x[j + u], a1[u & 3]);
-        }
-        for (; j + 3 <= q; j += 4) {
-            double aq[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) aq[u] = A[q + (int64_t)(j + u) * lda];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) a1[u] = fma(aq[u], x[j + u], a1[u]);
-        }
-        for (; j <= q; ++j) a1[0] = fma(A[q + (int64_t)j * lda], x[j], a1[0]);
-        y[p] = (a0[0] + a0[1]) + (a0[2] + a0[3]);
-        if (q != p) y[q] = (a1[0] + a1[1]) + (a1[2] + a1[3]);
     }
     __syncthreads();
-    // strictly lower columns: a warp takes four columns at a time (i, i+8, i+16, i+24), lanes over
-    // rows, two 32-row chunks of each column in flight
-    for (int i0 = warp; i0 < n; i0 += 4 * kWarps) {
-        double acc[4][2] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
-        int const base = i0 + 1 + lane;  // first row below column i0 for this lane
-        for (int j = base; j < n; j += 64) {
-            double a[4][2];
+    for (int i = tid; i < n; i += kThreads) {
+        double s = 0.0;
 #pragma unroll
-            for (int u = 0; u < 4; ++u)
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    int const i = i0 + kWarps * u, jj = j + 32 * h;
-                    a[u][h] = (i < n && jj > i && jj < n) ? A[jj + (int64_t)i * lda] : 0.0;
-                }
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    int const jj = j + 32 * h;
-                    acc[u][h] = fma(a[u][h], jj < n ? x[jj] : 0.0, acc[u][h]);
-                }
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            int const i = i0 + kWarps * u;
-            double s = acc[u][0] + acc[u][1];
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-            if (lane == 0 && i < n) y[i] += s;
-        }
+        for (int w = 0; w < kWarps; ++w) s += part[w * NMAX + i];
+        y[i] = s;
     }
     __syncthreads();
 }
@@ -656,7 +632,7 @@ __global__ void __launch_bounds__(kThreads, 2) posv_cta_mixed_kernel(Batch batch
         int it_count = 0;
         while (info == 0) {
             // r = b - A x (binary64)
-            cta_symv_lower(n, it.A, it.lda, x, r);
+            cta_symv_lower<NMAX>(n, it.A, it.lda, x, r, reinterpret_cast<double*>(buf));
             double rm = 0.0, xm = 0.0;
             for (int i = tid; i < n; i += kThreads) {
                 r[i] = bb[i] - r[i];
