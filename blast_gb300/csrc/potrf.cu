@@ -173,15 +173,18 @@ __device__ __forceinline__ void potrf_tile(int n, int k, int i, int nc, Src cons
 // TS rows (dense: KN = TS = 4, dense/Potrf.hpp:87-105; panel: KN = min((RC-4)/3, SS), TS = SS,
 // panel/Potrf.hpp:84-105). Returns info (0 or first bad pivot + 1).
 struct NoStripHook {
-    __device__ __forceinline__ void operator()(int, int) const {}
+    __device__ __forceinline__ void before(int, int) const {}
+    __device__ __forceinline__ void after(int, int) const {}
 };
 
-// after_strip(k, nc) runs once columns k .. k+nc-1 of L are final.
+// hook.before(k, nc) runs before strip k reads its columns, hook.after(k, nc) once columns
+// k .. k+nc-1 of L are final.
 template <int KN, int TS, class Src, class Addr, class Hook = NoStripHook>
-__device__ int potrf_thread_src(int n, Src const& A, double* L, Addr il, Hook const& after_strip = Hook{}) {
+__device__ int potrf_thread_src(int n, Src const& A, double* L, Addr il, Hook const& hook = Hook{}) {
     int info = 0;
     for (int k = 0; k < n; k += KN) {
         int const nc = min(KN, n - k);
+        hook.before(k, nc);
         double y[KN];
         int i = k;
         while (i < n) {
@@ -203,7 +206,7 @@ __device__ int potrf_thread_src(int n, Src const& A, double* L, Addr il, Hook co
                 i += TS;
             }
         }
-        after_strip(k, nc);
+        hook.after(k, nc);
     }
     return info;
 }
@@ -363,13 +366,58 @@ __device__ __forceinline__ void warp_copy_lower_cols(int n, int j0, int nc, int 
                 H[m * sh + i + (int64_t)j * ldh] = W[m * sw + i + (int64_t)j * ldw];
 }
 
-struct StripCopyOut {
-    int n, cnt, lane;
-    const double* W; int ldw; int64_t sw;
-    double* H; int ldh; int64_t sh;
-    __device__ __forceinline__ void operator()(int k, int nc) const {
+// Copies columns j0 .. j0+nc-1 (nc <= 4) of `cnt` consecutive instances from S to D, rows from j
+// (lower) or from 0, one warp, lanes over rows. For n <= 64 the loads of 4 instances (up to 32 per
+// lane) are issued together before their stores, so that a copy from host memory pays the link's
+// latency once per 4 instances.
+__device__ __forceinline__ void warp_stage_cols(int n, int j0, int nc, bool lower, int cnt, const double* S, int lds,
+                                                int64_t ss, double* D, int ldd, int64_t sd, int lane) {
+    if (n <= 64) {
+        for (int m0 = 0; m0 < cnt; m0 += 4) {
+            double v[4][4][2];
+#pragma unroll
+            for (int mm = 0; mm < 4; ++mm)
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        int const m = m0 + mm, j = j0 + c, i = (lower ? j : 0) + lane + 32 * h;
+                        v[mm][c][h] = (m < cnt && c < nc && i < n) ? S[m * ss + i + (int64_t)j * lds] : 0.0;
+                    }
+#pragma unroll
+            for (int mm = 0; mm < 4; ++mm)
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        int const m = m0 + mm, j = j0 + c, i = (lower ? j : 0) + lane + 32 * h;
+                        if (m < cnt && c < nc && i < n) D[m * sd + i + (int64_t)j * ldd] = v[mm][c][h];
+                    }
+        }
+    } else {
+        for (int m = 0; m < cnt; ++m)
+            for (int j = j0; j < j0 + nc; ++j)
+                for (int i = (lower ? j : 0) + lane; i < n; i += 32)
+                    D[m * sd + i + (int64_t)j * ldd] = S[m * ss + i + (int64_t)j * lds];
+    }
+}
+
+// Strip hooks of the mirror kernel (a full warp of 32 instances): before strip k the warp stages
+// the strip's columns of A from host memory into the device working copy (where the tiles then
+// read them, the factorisation running in place), after it the finished columns of L go back.
+struct MirrorHook {
+    int n, lane;
+    const double* Ah; int ldah; int64_t sah;
+    double* W; int ldw; int64_t sw;
+    double* Lh; int ldlh; int64_t slh;
+    __device__ __forceinline__ void before(int k, int nc) const {
         __syncwarp();
-        warp_copy_lower_cols(n, k, nc, cnt, W, ldw, sw, H, ldh, sh, lane);
+        warp_stage_cols(n, k, nc, true, 32, Ah, ldah, sah, W, ldw, sw, lane);
+        __syncwarp();
+    }
+    __device__ __forceinline__ void after(int k, int nc) const {
+        __syncwarp();
+        warp_copy_lower_cols(n, k, nc, 32, W, ldw, sw, Lh, ldlh, slh, lane);
     }
 };
 
@@ -380,19 +428,26 @@ __global__ void __launch_bounds__(32, 12) posv_mirror_kernel(PosvArgs p, MirrorO
     int const n = p.n;
     bool const full = b0 + 32 <= p.batch;  // warp-uniform
     int const cnt = full ? 32 : (int)(p.batch - b0);
-    if (full) {  // L leaves strip by strip
+    if (full) {  // A arrives and L leaves strip by strip, in whole-warp copies
         double* L = p.L + b * p.sl;
-        StripCopyOut const out{n, 32, lane, p.L + b0 * p.sl, p.ldl, p.sl, o.Lh + b0 * o.slh, o.ldlh, o.slh};
-        int const info = potrf_thread_src<4, 4>(n, LoadSrc<ColAddr>{p.A + b * p.sa, ColAddr{p.lda}}, L,
-                                                ColAddr{p.ldl}, out);
+        MirrorHook const hook{n,     lane,  p.A + b0 * p.sa,  p.lda,  p.sa,  p.L + b0 * p.sl,
+                              p.ldl, p.sl,  o.Lh + b0 * o.slh, o.ldlh, o.slh};
+        int const info = potrf_thread_src<4, 4>(n, LoadSrc<ColAddr>{L, ColAddr{p.ldl}}, L, ColAddr{p.ldl}, hook);
         if (p.info) p.info[b] = info;
+        if (p.nrhs > 0) {  // B staged into the working copy of X, then solved in place
+            __syncwarp();
+            for (int j0 = 0; j0 < p.nrhs; j0 += 4)
+                warp_stage_cols(n, j0, min(4, p.nrhs - j0), false, 32, p.B + b0 * p.sb, p.ldb, p.sb, p.X + b0 * p.sx,
+                                p.ldx, p.sx, lane);
+            __syncwarp();
+            double* X = p.X + b * p.sx;
+            trsm_lower_thread(n, p.nrhs, L, p.ldl, X, p.ldx, X, p.ldx);
+            trsm_lower_trans_thread(n, p.nrhs, L, p.ldl, X, p.ldx);
+        }
     } else if (b < p.batch) {
         double* L = p.L + b * p.sl;
         int const info = potrf_thread<4, 4>(n, p.A + b * p.sa, ColAddr{p.lda}, L, ColAddr{p.ldl});
         if (p.info) p.info[b] = info;
-    }
-    if (b < p.batch) {
-        double* L = p.L + b * p.sl;
         if (p.nrhs > 0) {
             double* X = p.X + b * p.sx;
             trsm_lower_thread(n, p.nrhs, L, p.ldl, p.B + b * p.sb, p.ldb, X, p.ldx);
