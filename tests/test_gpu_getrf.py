@@ -194,3 +194,26 @@ def test_gesv_plan_log_uniform(gpu, oracle_lib):
         oracle_lib.getrs(LUr, pr, xr, xr)
         assert np.array_equal(p, pr), n
         assert np.array_equal(x, xr), n
+
+
+@pytest.mark.parametrize("n", [300, 513, 800])
+def test_getrs_large_n_bitexact(gpu, oracle_lib, n):
+    """getrs beyond the ragged workload's sizes: the solution vectors take 32 n doubles of shared
+    memory per warp (200 KB at the n = 800 limit); bit-identical to the oracle."""
+    import torch
+
+    rng = np.random.default_rng(n)
+    batch, nrhs = 3, 2
+    A = rng.standard_normal((batch, n, n))
+    B = rng.standard_normal((batch, n, nrhs))
+    dA, dB = to_dev(A), to_dev(B)
+    ipiv = torch.zeros((batch, n), dtype=torch.int32, device="cuda")
+    info = gpu.getrf(dA, ipiv)
+    gpu.getrs(dA, ipiv, dB, info)
+    torch.cuda.synchronize()
+    X = dB.cpu().numpy()
+    for b in range(batch):
+        LUr, pr, _ = _oracle_lu(oracle_lib, A[b])
+        Xr = np.asfortranarray(B[b].copy())
+        oracle_lib.getrs(LUr, pr, Xr, Xr)
+        assert np.array_equal(X[b], Xr), n

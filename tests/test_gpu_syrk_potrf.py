@@ -102,3 +102,21 @@ def test_syrk_potrf_argument_errors(gpu):
     with pytest.raises(ValueError):
         gpu.syrk_potrf(1.0, to_dev(np.zeros((2, 4, 3))), 1.0, to_dev(np.zeros((2, 5, 5))),
                        to_dev(np.zeros((2, 5, 5))))
+
+
+def test_syrk_potrf_k0_is_potrf(gpu, path):
+    """k = 0 leaves D = chol(beta*C); with beta = 1 it is potrf(C) bit for bit."""
+    import torch
+
+    rng = np.random.default_rng(34)
+    batch, n = 40, 24
+    _, C = _case(rng, batch, n, 1)
+    dC = to_dev(C)
+    dA = torch.zeros((batch, n, 0), dtype=torch.float64, device="cuda")
+    dD = to_dev(np.zeros((batch, n, n)))
+    info = gpu.syrk_potrf(1.0, dA, 1.0, dC, dD)
+    dL = to_dev(np.zeros((batch, n, n)))
+    info2 = gpu.potrf(dC, dL)
+    torch.cuda.synchronize()
+    assert not info.any() and not info2.any()
+    assert torch.equal(torch.tril(dD), torch.tril(dL))
