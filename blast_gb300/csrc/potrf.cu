@@ -357,15 +357,6 @@ struct MirrorOut {
     double* Xh; int ldxh; int64_t sxh;
 };
 
-// Copies rows j .. n-1 of columns j0 .. j0+nc-1 of `cnt` consecutive instances, one warp.
-__device__ __forceinline__ void warp_copy_lower_cols(int n, int j0, int nc, int cnt, const double* W, int ldw,
-                                                     int64_t sw, double* H, int ldh, int64_t sh, int lane) {
-    for (int m = 0; m < cnt; ++m)
-        for (int j = j0; j < j0 + nc; ++j)
-            for (int i = j + lane; i < n; i += 32)
-                H[m * sh + i + (int64_t)j * ldh] = W[m * sw + i + (int64_t)j * ldw];
-}
-
 // Copies columns j0 .. j0+nc-1 (nc <= 4) of `cnt` consecutive instances from S to D, rows from j
 // (lower) or from 0, one warp, lanes over rows. For n <= 64 the loads of 4 instances (up to 32 per
 // lane) are issued together before their stores, so that a copy from host memory pays the link's
@@ -402,6 +393,15 @@ __device__ __forceinline__ void warp_stage_cols(int n, int j0, int nc, bool lowe
     }
 }
 
+// Copies rows j .. n-1 (lower) or 0 .. n-1 of columns j0 .. j0+nc-1 (any nc) of `cnt` consecutive
+// instances, one warp, through warp_stage_cols' batched loads: a copy to host memory then waits on
+// the source's latency once per batch instead of once per element.
+__device__ __forceinline__ void warp_copy_cols(int n, int j0, int nc, bool lower, int cnt, const double* W, int ldw,
+                                               int64_t sw, double* H, int ldh, int64_t sh, int lane) {
+    for (int j = j0; j < j0 + nc; j += 4)
+        warp_stage_cols(n, j, min(4, j0 + nc - j), lower, cnt, W, ldw, sw, H, ldh, sh, lane);
+}
+
 // Strip hooks of the mirror kernel (a full warp of 32 instances): before strip k the warp stages
 // the strip's columns of A from host memory into the device working copy (where the tiles then
 // read them, the factorisation running in place), after it the finished columns of L go back.
@@ -417,7 +417,7 @@ struct MirrorHook {
     }
     __device__ __forceinline__ void after(int k, int nc) const {
         __syncwarp();
-        warp_copy_lower_cols(n, k, nc, 32, W, ldw, sw, Lh, ldlh, slh, lane);
+        warp_copy_cols(n, k, nc, true, 32, W, ldw, sw, Lh, ldlh, slh, lane);
     }
 };
 
@@ -456,14 +456,9 @@ __global__ void __launch_bounds__(32, 12) posv_mirror_kernel(PosvArgs p, MirrorO
     }
     __syncwarp();
     if (!full)
-        warp_copy_lower_cols(n, 0, n, cnt, p.L + b0 * p.sl, p.ldl, p.sl, o.Lh + b0 * o.slh, o.ldlh, o.slh, lane);
-    if (p.nrhs == 0) return;
-    for (int m = 0; m < cnt; ++m) {
-        const double* X = p.X + (b0 + m) * p.sx;
-        double* Xh = o.Xh + (b0 + m) * o.sxh;
-        for (int j = 0; j < p.nrhs; ++j)
-            for (int i = lane; i < n; i += 32) Xh[i + (int64_t)j * o.ldxh] = X[i + (int64_t)j * p.ldx];
-    }
+        warp_copy_cols(n, 0, n, true, cnt, p.L + b0 * p.sl, p.ldl, p.sl, o.Lh + b0 * o.slh, o.ldlh, o.slh, lane);
+    if (p.nrhs > 0)
+        warp_copy_cols(n, 0, p.nrhs, false, cnt, p.X + b0 * p.sx, p.ldx, p.sx, o.Xh + b0 * o.sxh, o.ldxh, o.sxh, lane);
 }
 
 // Ragged potrf over descriptors whose matrices all have the layout `layout` (column-major, or

@@ -23,8 +23,9 @@ def _inputs(rng, batch, n, nrhs):
 
 @pytest.mark.parametrize("transport", ["copy", "direct", "mirror"])
 @pytest.mark.parametrize("n,nrhs,batch,chunk", [(48, 8, 1000, 300), (17, 3, 257, 257), (5, 1, 70, 32),
-                                                (64, 0, 40, 16)])
+                                                (64, 0, 40, 16), (48, 8, 20000, 20000), (8, 3, 48657, 48657)])
 def test_host_pipeline_matches_device_posv(gpu, transport, n, nrhs, batch, chunk):
+    """The last two sizes run ten or more warps per SM (the last one partial in the second)."""
     import torch
 
     from blast_gb300.host import PosvHostPipeline, pinned_col_major
