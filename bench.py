@@ -395,11 +395,15 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded N(0,1), generated on device)",
         "config": {"workload": WORKLOAD, "batch_per_gpu": BATCH, "n": N, "nrhs": NRHS,
-                   "parallelism": f"replicas x{ws}", "l2": "inputs 1.07 GB > L2, no flush"},
+                   "parallelism": f"replicas x{ws}",
+                   "l2": f"inputs {BATCH * (N * N + N * NRHS) * 8 / 1e9:.2f} GB"
+                         + (" > L2 (129 MB), no flush" if BATCH * (N * N + N * NRHS) * 8 > 129e6 else ", L2-resident")},
         "gflops": value * FLOPS_PER / 1e9,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None,
-                     "traffic": traffic.get("bytes_per_launch") if traffic else None,
+                     # the capture's DRAM bytes hold for the captured batch only
+                     "traffic": traffic.get("bytes_per_launch") if traffic and traffic.get("batch") == BATCH
+                     else None,
                      "algorithmic_bytes": BATCH * BYTES_PER,
                      "peak_source": "binary64 FMA probe kernel run in this process (MEASURED_PEAKS.json has no FP64 figure)",
                      "kernel": "posv_thread_kernel"},
