@@ -39,8 +39,8 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kNB = 32;  // panel width = 4 columns per warp
-constexpr int kKC = 32;  // previous columns staged per pass of the panel update (= panel width,
-                         // so the staging buffer fits in the panel buffer's space)
+constexpr int kKC = 32;  // previous columns staged at once by the panel update, as two chunks of 16
+                         // (= panel width, so the staging buffer fits in the panel buffer's space)
 
 struct CtaItem {
     int n;
@@ -62,7 +62,7 @@ struct DescPosv {
     }
 };
 
-// Asynchronous global -> shared copies (cp.async, completed by cp_async_wait_all + a barrier):
+// Asynchronous global -> shared copies (cp.async, completed by cp.async.wait_group + a barrier):
 // every thread issues all of its copies back to back instead of waiting for each load.
 __device__ __forceinline__ void cp_async(float* dst, const float* src) {
     unsigned const d = (unsigned)__cvta_generic_to_shared(dst);
@@ -72,7 +72,6 @@ __device__ __forceinline__ void cp_async(double* dst, const double* src) {
     unsigned const d = (unsigned)__cvta_generic_to_shared(dst);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
 }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 template <typename T>
 __device__ __forceinline__ T rsqrt_t(T s);
@@ -102,27 +101,45 @@ struct Smem {
 };
 
 // Update of the panel's register tiles with all previous columns: acc -= F(k0:n, kk) * F(k0+c, kk)
-// for kk < k0, the columns streamed through shared memory kKC at a time. RA = row blocks still
-// below the diagonal (ceil(m / 32)), fixed at compile time so that the inner loop is RA x 4
-// fused multiply-adds with no per-row guards. Rows past m and columns past nb pick up stale
-// shared-memory values; they are never stored.
+// for kk < k0, the columns streamed through shared memory in chunks of kKC / 2, double-buffered:
+// the next chunk's asynchronous copies are in flight while the current chunk is applied. RA = row
+// blocks still below the diagonal (ceil(m / 32)), fixed at compile time so that the inner loop is
+// RA x 4 fused multiply-adds with no per-row guards. Rows past m and columns past nb pick up
+// stale shared-memory values; they are never stored.
+template <typename T, int MAXR>
+__device__ __forceinline__ void panel_stage(const T* F, int ldf, T* buf, int k0, int m, int ch) {
+    constexpr int NMAX = 32 * MAXR, KH = kKC / 2;
+    int const kk = ch * KH, kc = min(KH, k0 - kk);
+    T* dst = buf + (ch & 1) * KH * NMAX;
+    for (int q = 0; q < kc; ++q) {
+        T const* src = F + k0 + (int64_t)(kk + q) * ldf;
+        for (int r = threadIdx.x; r < m; r += kThreads) cp_async(dst + q * NMAX + r, src + r);
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
 template <typename T, int RA, int MAXR>
 __device__ __forceinline__ void panel_update(T (&acc)[MAXR][4], const T* F, int ldf, T* buf, int k0, int m,
                                              int c0) {
-    constexpr int NMAX = 32 * MAXR;
-    int const tid = threadIdx.x, lane = tid & 31;
-    for (int kk = 0; kk < k0; kk += kKC) {
-        int const kc = min(kKC, k0 - kk);
-        __syncthreads();
-        for (int q = 0; q < kc; ++q) {
-            T const* src = F + k0 + (int64_t)(kk + q) * ldf;
-            for (int r = tid; r < m; r += kThreads) cp_async(buf + q * NMAX + r, src + r);
+    constexpr int NMAX = 32 * MAXR, KH = kKC / 2;
+    int const lane = threadIdx.x & 31;
+    int const nch = (k0 + KH - 1) / KH;
+    if (nch == 0) return;
+    __syncthreads();  // the buffer's earlier contents are no longer read
+    panel_stage<T, MAXR>(F, ldf, buf, k0, m, 0);
+    for (int ch = 0; ch < nch; ++ch) {
+        if (ch + 1 < nch) {
+            panel_stage<T, MAXR>(F, ldf, buf, k0, m, ch + 1);  // into the half chunk ch - 1 used
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         }
-        cp_async_wait_all();
         __syncthreads();
+        int const kc = min(KH, k0 - ch * KH);
+        T const* base = buf + (ch & 1) * KH * NMAX;
 #pragma unroll 2
         for (int q = 0; q < kc; ++q) {
-            T const* col = buf + q * NMAX;
+            T const* col = base + q * NMAX;
             T b[4];
 #pragma unroll
             for (int j = 0; j < 4; ++j) b[j] = col[c0 + j];
@@ -133,6 +150,7 @@ __device__ __forceinline__ void panel_update(T (&acc)[MAXR][4], const T* F, int 
                 for (int j = 0; j < 4; ++j) acc[i][j] = fma(-a, b[j], acc[i][j]);
             }
         }
+        __syncthreads();  // every thread is done with this half before chunk ch + 2 is staged into it
     }
 }
 
@@ -281,26 +299,31 @@ __device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf,
         int const m = n - k0;
         int const c0 = warp * 4;  // this warp's panel columns c0..c0+3 (relative to k0)
         T acc[MAXR][4];
-        float csum[4] = {0.f, 0.f, 0.f, 0.f};  // |a| below the diagonal, per panel column
+        // All of the panel's loads are issued before any use, so that they overlap.
 #pragma unroll
         for (int i = 0; i < MAXR; ++i) {
             int const r = lane + 32 * i;  // row relative to k0
-            float rs = 0.f;  // binary32 sums: |A|_inf only scales the backward error
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 int const c = c0 + j;
-                double const v = (r < m && c < nb && r >= c) ? A[(k0 + r) + (int64_t)(k0 + c) * lda] : 0.0;
-                acc[i][j] = (T)v;
-                if (rowsum) {
-                    float const av = fabsf((float)v);
-                    rs += av;
-                    if (r > c) csum[j] += av;
-                }
+                acc[i][j] = (T)((r < m && c < nb && r >= c) ? A[(k0 + r) + (int64_t)(k0 + c) * lda] : 0.0);
             }
-            if (rowsum && r < m) reinterpret_cast<double*>(buf)[warp * NMAX + r] = rs;
         }
         if (rowsum) {
             double* part = reinterpret_cast<double*>(buf);  // [kWarps][NMAX] rows, then [kNB] columns
+            float csum[4] = {0.f, 0.f, 0.f, 0.f};  // |a| below the diagonal, per panel column
+#pragma unroll
+            for (int i = 0; i < MAXR; ++i) {
+                int const r = lane + 32 * i;
+                float rs = 0.f;  // binary32 sums: |A|_inf only scales the backward error
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    float const av = fabsf((float)acc[i][j]);  // (float)acc[i][j] == (float)a_rc for T float or double
+                    rs += av;
+                    if (r > c0 + j) csum[j] += av;
+                }
+                if (r < m) part[warp * NMAX + r] = rs;
+            }
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 float v = csum[j];
@@ -356,10 +379,17 @@ __device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf,
             }
         }
         __syncthreads();
-        // Panel to the factor (lower part).
-        for (int c = 0; c < nb; ++c) {
-            T* dst = F + k0 + (int64_t)(k0 + c) * ldf;
-            for (int r = c + tid; r < m; r += kThreads) dst[r] = buf[c * NMAX + r];
+        // Panel to the factor (lower part), four columns per pass with their shared-memory loads
+        // issued before the stores.
+        for (int cb = 0; cb < nb; cb += 4) {
+            for (int r = cb + tid; r < m; r += kThreads) {
+                T v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) v[u] = (cb + u < nb && r >= cb + u) ? buf[(cb + u) * NMAX + r] : (T)0;
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (cb + u < nb && r >= cb + u) F[(k0 + r) + (int64_t)(k0 + cb + u) * ldf] = v[u];
+            }
         }
         __syncthreads();
     }
