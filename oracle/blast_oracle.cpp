@@ -182,10 +182,11 @@ int potrf_impl(int M, int N, MA A, ML L, int kn, int tile) {
     return info;
 }
 
-// Column-major Cholesky for the batch driver, shaped like BLAST's kernel (dense/Potrf.hpp:20-106):
-// per strip of 4 columns, register tiles of KM = 12/8/4 rows whose inner loops run over
-// contiguous rows, so the compiler vectorises them the way BLAST's SIMD tiles are. Same
-// per-element operations, in the same order, as potrf_impl (tile = kn = 4): bitwise identical.
+// Column-major Cholesky for the batched entry point (oracle_dposv_batch), shaped like BLAST's
+// kernel (dense/Potrf.hpp:20-106): per strip of 4 columns, register tiles of KM = 12/8/4 rows
+// whose inner loops run over contiguous rows, so the compiler vectorises them the way BLAST's
+// SIMD tiles are. Same per-element operations, in the same order, as potrf_impl (tile = kn = 4):
+// bitwise identical.
 template <int KM>
 void potrf_tile_col(int n, int k, int i, int nc, const double* A, int64_t lda, double* L, int64_t ldl,
                     double* sq, bool diag, int& info) {
@@ -249,7 +250,7 @@ int potrf_col(int n, const double* A, int64_t lda, double* L, int64_t ldl) {
     return info;
 }
 
-// The two solves of potrs for the batch driver, vectorised across right-hand sides with a
+// The two solves of potrs for the batched entry point, vectorised across right-hand sides with a
 // row-major scratch copy of X; per element the same order as trsm_impl (dense/Trsm.hpp:39-65).
 constexpr int kMaxRhs = 8;
 void potrs_col(int n, int nrhs, const double* L, int64_t ldl, const double* B, int64_t ldb,
