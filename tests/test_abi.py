@@ -70,3 +70,80 @@ def test_argument_validation_without_device(lib):
                                       None) == -2
     with pytest.raises(_lib.BlastGpuError):
         _lib.call("blastgpu_dpotrs_strided", -1, 1, None, 1, 0, None, 1, 0, None, 1, 0, 1, None)
+
+
+def test_argument_validation_blas2_and_extensions(lib):
+    """The BLAS-2 entry points, the right-side solve, the fused Riccati step and the host-operand
+    solve check their arguments on the host in declaration order. Every case below fails a check
+    that precedes any CUDA call. The fake pointer (8) is never dereferenced, because a later
+    argument is invalid."""
+    p = 8  # non-null stand-in for a pointer argument that is checked only for null
+    ger = lib.blastgpu_dger_strided
+    assert ger(-1, 1, 1.0, None, 1, 0, None, 1, 0, None, 1, 0, None, 1, 0, 1, None) == -1
+    assert ger(1, -1, 1.0, None, 1, 0, None, 1, 0, None, 1, 0, None, 1, 0, 1, None) == -2
+    assert ger(2, 2, 1.0, None, 1, 0, None, 1, 0, None, 2, 0, None, 2, 0, 1, None) == -4
+    assert ger(0, 0, 1.0, None, 0, 0, None, 1, 0, None, 1, 0, None, 1, 0, 1, None) == -5
+    assert ger(0, 0, 1.0, None, 1, 0, None, 0, 0, None, 1, 0, None, 1, 0, 1, None) == -8
+    assert ger(3, 2, 1.0, p, 1, 0, p, 1, 0, p, 2, 0, p, 3, 0, 1, None) == -11
+    assert ger(3, 2, 1.0, p, 1, 0, p, 1, 0, p, 3, 0, p, 2, 0, 1, None) == -14
+    assert ger(3, 2, 1.0, p, 1, 0, p, 1, 0, p, 3, 0, p, 3, 0, -1, None) == -16
+    assert ger(0, 5, 1.0, None, 1, 0, None, 1, 0, None, 1, 0, None, 1, 0, 7, None) == 0  # empty: no-op
+
+    iamax = lib.blastgpu_idamax_strided
+    assert iamax(0, p, 1, 0, p, 1, None) == -1  # BLAST asserts a non-empty vector
+    assert iamax(4, None, 1, 0, p, 1, None) == -2
+    assert iamax(4, p, 0, 0, p, 1, None) == -3
+    assert iamax(4, p, 1, 0, None, 1, None) == -5
+    assert iamax(4, p, 1, 0, p, -1, None) == -6
+
+    laswp = lib.blastgpu_dlaswp_strided
+    assert laswp(-1, None, 1, 0, 0, 0, None, 0, 1, None) == -1
+    assert laswp(0, None, 0, 0, 0, 0, None, 0, 1, None) == -3
+    assert laswp(2, p, 4, 0, -1, 0, None, 0, 1, None) == -5
+    assert laswp(2, p, 4, 0, 3, 2, None, 0, 1, None) == -6
+    assert laswp(2, p, 4, 0, 0, 2, None, 0, 1, None) == -7
+    assert laswp(2, p, 4, 0, 0, 2, p, 4, -1, None) == -9
+
+    swap = lib.blastgpu_dswap_strided
+    assert swap(-1, None, 1, 0, None, 1, 0, 1, None) == -1
+    assert swap(0, None, 0, 0, None, 1, 0, 1, None) == -3
+    assert swap(0, None, 1, 0, None, 0, 0, 1, None) == -6
+    assert swap(3, p, 1, 0, p, 1, 0, -1, None) == -8
+
+    tr = lib.blastgpu_dtrsm_right_strided
+    assert tr(7, 0, 0, 1, 1, p, 1, 0, p, 1, 0, p, 1, 0, 1, None) == -1
+    assert tr(0, 2, 0, 1, 1, p, 1, 0, p, 1, 0, p, 1, 0, 1, None) == -2
+    assert tr(0, 0, 2, 1, 1, p, 1, 0, p, 1, 0, p, 1, 0, 1, None) == -3
+    assert tr(0, 0, 0, 3, 4, p, 3, 0, p, 3, 0, p, 3, 0, 1, None) == -7  # lda < n
+    assert tr(0, 0, 0, 3, 4, p, 4, 0, p, 2, 0, p, 3, 0, 1, None) == -10  # ldb < m
+    assert tr(0, 0, 0, 3, 4, p, 4, 0, p, 3, 0, None, 3, 0, 1, None) == -12
+    assert tr(0, 0, 0, 3, 4, p, 4, 0, p, 3, 0, p, 3, 0, -2, None) == -15
+
+    sp = lib.blastgpu_dsyrk_potrf_strided
+    assert sp(-1, 1, 0, 1.0, p, 1, 0, 1.0, p, 1, 0, p, 1, 0, None, 1, None) == -1
+    assert sp(4, -1, 0, 1.0, p, 4, 0, 1.0, p, 4, 0, p, 4, 0, None, 1, None) == -2
+    assert sp(4, 2, 2, 1.0, p, 4, 0, 1.0, p, 4, 0, p, 4, 0, None, 1, None) == -3
+    assert sp(4, 2, 0, 1.0, None, 4, 0, 1.0, p, 4, 0, p, 4, 0, None, 1, None) == -5
+    assert sp(4, 2, 1, 1.0, p, 1, 0, 1.0, p, 4, 0, p, 4, 0, None, 1, None) == -6  # trans: lda >= k
+    assert sp(4, 2, 0, 1.0, p, 4, 0, 1.0, p, 4, 0, None, 4, 0, None, 1, None) == -12
+    assert sp(4, 2, 0, 1.0, p, 4, 0, 1.0, p, 4, 0, p, 4, 0, None, -1, None) == -16
+
+    mirror = lib.blastgpu_dposv_mirror_strided
+    # n, nrhs, A, lda, sa, B, ldb, sb, L, ldl, sl, X, ldx, sx, L_work, X_work, info, batch, stream
+    ok = (48, 8, p, 48, 0, p, 48, 0, p, 48, 0, p, 48, 0, p, p, None, 1, None)
+
+    def call(**bad):
+        args = list(ok)
+        for i, v in bad.items():
+            args[int(i[1:])] = v
+        return mirror(*args)
+
+    assert call(a0=-1) == -1
+    assert call(a1=-1) == -2
+    assert call(a2=None) == -3
+    assert call(a3=47) == -4
+    assert call(a5=None) == -6
+    assert call(a9=40) == -10
+    assert call(a14=None) == -15  # the device workspace for L
+    assert call(a15=None) == -16  # the device workspace for X
+    assert call(a17=-1) == -18
