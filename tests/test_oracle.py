@@ -213,6 +213,61 @@ def test_trmm_sweep(orc):
     assert orc.trmm(0, 1, 1, 1.0, A, A, F(np.zeros((3, 3)))) == -100
 
 
+def test_trmm_any_and_trsm_right_against_numpy(orc):
+    """The oracle's extensions beyond BLAST (no reference algorithm, so pinned by the definition):
+    every (side, uplo, unit) trmm is alpha * tri(A) * B or alpha * B * tri(A), reading only the
+    named triangle (unit: an implicit 1 diagonal); the right-side solve X op(A) = B with op(A)
+    triangular (uplo and unit describe op(A))."""
+    rng = np.random.default_rng(12)
+
+    def tri(A, uplo, unit):
+        T = np.triu(A) if uplo else np.tril(A)
+        if unit:
+            np.fill_diagonal(T, 1.0)
+        return T
+
+    for m, n in [(1, 1), (3, 5), (7, 2), (12, 12), (20, 9)]:
+        for side in (0, 1):
+            for uplo in (0, 1):
+                for unit in (0, 1):
+                    k = m if side == 0 else n
+                    A = F(rng.random((k, k)) + 9.0 * (1 - unit) * np.eye(k))
+                    A_junk = A.copy()  # the other triangle (and a unit diagonal) must not be read
+                    other = np.tril_indices(k, -1) if uplo else np.triu_indices(k, 1)
+                    A_junk[other] = np.nan
+                    if unit:
+                        np.fill_diagonal(A_junk, np.nan)
+                    B = F(rng.random((m, n)))
+                    C = F(np.zeros((m, n)))
+                    alpha = float(rng.uniform(0.5, 2))
+                    assert orc.trmm_any(side, uplo, unit, alpha, F(A_junk), B, C) == 0
+                    want = alpha * (tri(A, uplo, unit) @ B if side == 0 else B @ tri(A, uplo, unit))
+                    assert approx_equal(C, want, 1e-12, 1e-12), (m, n, side, uplo, unit)
+        for uplo in (0, 1):
+            for unit in (0, 1):
+                for trans in (0, 1):
+                    A = F(rng.random((n, n)) + 4.0 * np.eye(n))
+                    B = F(rng.random((m, n)))
+                    X = F(np.zeros((m, n)))
+                    assert orc.trsm_right(uplo, unit, A, B, X, trans) == 0
+                    T = tri(A.T if trans else A, uplo, unit)  # uplo describes op(A), as in BLAST's trsm
+                    assert approx_equal(X @ T, B, 1e-12, 1e-12), (m, n, uplo, unit, trans)
+
+
+def test_laswp_against_numpy(orc):
+    """blast::laswp (dense/Laswp.hpp:37-43): for k = k0..k1-1 swap rows k and ipiv[k]."""
+    rng = np.random.default_rng(13)
+    m, ncols = 17, 6
+    for k0, k1 in [(0, 17), (3, 11), (5, 5)]:
+        A = F(rng.random((m, ncols)))
+        ipiv = np.array([rng.integers(k, m) for k in range(m)], dtype=np.int32)
+        want = A.copy()
+        for k in range(k0, k1):
+            want[[k, ipiv[k]]] = want[[ipiv[k], k]]
+        orc.laswp(A, k0, k1, ipiv)
+        assert np.array_equal(A, want)
+
+
 def test_iamax(orc):
     """dense/Iamax.cpp:25-38 plus the scan's tie and NaN rules (dense/Iamax.hpp:82-95)."""
     rng = np.random.default_rng(9)
