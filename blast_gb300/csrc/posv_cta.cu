@@ -10,13 +10,15 @@
 //  * Factorisation, left-looking with panels of 32 columns. Warp w owns panel columns
 //    4w..4w+3, lane l owns rows l, l+32, ..., so each thread keeps an MAXR x 4 register tile
 //    (BLAST's RegisterMatrix, 32 times wider). The update of a panel with all previous columns
-//    streams those columns through shared memory 32 at a time; every thread then performs
-//    RA*4 fused multiply-adds per column (RA = 32-row blocks still below the diagonal, fixed at
+//    streams those columns through shared memory with cp.async, 16 at a time and double-buffered
+//    (the next 16 are in flight while the current ones are applied); every thread performs RA*4
+//    fused multiply-adds per column (RA = 32-row blocks still below the diagonal, fixed at
 //    compile time per panel) with operands read conflict-free from shared memory (rows:
 //    consecutive lanes; panel columns: a warp-uniform broadcast).
-//  * The 32 x 32 diagonal block is factored in place in shared memory (all threads; binary32 in
-//    sub-panels of 8 columns finished by warp 0 in registers), the rows below are solved against
-//    it (one thread per row), and the panel is written to the factor.
+//  * The 32 x 32 diagonal block is factored in place in shared memory: binary64 column at a time
+//    by all threads with warp 0 finishing each pivot column, binary32 in sub-panels of 8 columns
+//    factored by warp 0 in registers. The rows below are then solved against it (one thread per
+//    row), and the panel is written to the factor.
 //  * Forward and backward substitution run blockwise with look-ahead: once a 32-row block is
 //    solved, warp 0 applies it to the next block and solves that block's triangle from registers
 //    with shuffles while the other warps apply it to everything beyond; one barrier per block.
