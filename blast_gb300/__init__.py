@@ -5,13 +5,13 @@ build script, a ctypes binding, and ``blast``, a Python mirror of BLAST's functi
 torch device tensors.
 """
 from . import _lib
-from .blast import (LEFT, LOWER, RIGHT, UPPER, col_major, gemm, ger, getrf, getrs, iamax, laswp,
-                    posv, potrf, potrs, swap, syrk_lower, syrk_potrf, trmm, trsm, trsm_right, trsv_left_lower,
-                    trsv_left_upper)
+from .blast import (LEFT, LOWER, RIGHT, UPPER, col_major, gemm, gemm_bwd, ger, getrf, getrs, iamax, laswp,
+                    posv, potrf, potrf_bwd, potrs, swap, syrk_lower, syrk_potrf, trmm, trsm, trsm_bwd, trsm_right,
+                    trsv_left_lower, trsv_left_upper)
 
 __all__ = ["gemm", "potrf", "posv", "potrs", "getrf", "getrs", "syrk_lower", "syrk_potrf", "trsm", "trsm_right", "trmm", "ger",
-           "iamax", "laswp", "swap", "trsv_left_lower", "trsv_left_upper", "col_major", "LOWER",
-           "UPPER", "LEFT", "RIGHT", "_lib"]
+           "iamax", "laswp", "swap", "trsv_left_lower", "trsv_left_upper", "gemm_bwd", "trsm_bwd", "potrf_bwd",
+           "col_major", "LOWER", "UPPER", "LEFT", "RIGHT", "_lib"]
 
 
 def _apply_tuning():

@@ -78,6 +78,11 @@ SIGNATURES: dict[str, list] = {
     "blastgpu_dgesv_batched": [PTR, PTR, I64, I32, PTR],
     "blastgpu_dposv_mixed_workspace_bytes": [I32],
     "blastgpu_dsyrk_lower_strided": [I32, I32, DBL, PTR, I32, I64, DBL, PTR, I32, I64, PTR, I32, I64, I64, PTR],
+    "blastgpu_dgemm_bwd_strided": [I32, I32, I32, I32, I32, DBL, PTR, I32, I64, PTR, I32, I64, DBL, PTR, I32, I64,
+                                   PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, I64, PTR],
+    "blastgpu_dtrsm_bwd_strided": [I32, I32, I32, I32, I32, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, PTR, I32,
+                                   I64, PTR, I32, I64, I64, PTR],
+    "blastgpu_dpotrf_bwd_strided": [I32, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, I64, PTR],
     "blastgpu_dtrsm_strided": [I32, I32, I32, I32, I32, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, I64, PTR],
     "blastgpu_dtrmm_strided": [I32, I32, I32, I32, I32, DBL, PTR, I32, I64, PTR, I32, I64, PTR, I32, I64, I64, PTR],
     "blastgpu_dposv_batched": [PTR, I64, I32, PTR, PTR],

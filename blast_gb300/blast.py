@@ -316,6 +316,78 @@ def trsm_right(uplo: int, unit: bool, A: torch.Tensor, B: torch.Tensor, X: torch
     return X
 
 
+def _out(t, name: str, rows: int, cols: int, layout: int, batch: int):
+    """Pointer, ld and batch stride of an optional gradient output with the given shape and
+    storage orientation, holding the whole batch."""
+    if t is None:
+        return 0, 1, 0
+    o = _as_mat(t, name)
+    if o.rows != rows or o.cols != cols:
+        raise ValueError(f"{name} must have shape ({rows}, {cols})")
+    if o.layout != layout:
+        raise ValueError(f"{name} must have the storage order of its forward operand")
+    if o.batch != batch or (batch > 1 and o.bstride == 0):
+        raise ValueError(f"{name} must hold the whole batch")
+    return o.ptr, o.ld, o.bstride
+
+
+def gemm_bwd(alpha, A: torch.Tensor, B: torch.Tensor, beta, Dbar: torch.Tensor, Abar=None, Bbar=None,
+             Cbar=None):
+    """Adjoint of D = alpha*A*B + beta*C (gemm above): ACCUMULATES dl/dA into Abar, dl/dB into Bbar
+    and dl/dC into Cbar (each optional; same shape and storage order as A, B and C; zero them
+    first for plain gradients). A and B are the forward operands (row-major = BLAST's trans())."""
+    a, b, db = _as_mat(A, "A"), _as_mat(B, "B"), _as_mat(Dbar, "Dbar")
+    M, N, K = a.rows, b.cols, a.cols
+    if b.rows != K or db.rows != M or db.cols != N:
+        raise ValueError("Matrix sizes do not match")
+    _square_col(db, "Dbar")
+    batch = _batch_of(a, b, db)
+    oa = _out(Abar, "Abar", M, K, a.layout, batch)
+    ob = _out(Bbar, "Bbar", K, N, b.layout, batch)
+    oc = _out(Cbar, "Cbar", M, N, COL, batch)
+    _lib.call("blastgpu_dgemm_bwd_strided", int(a.layout == ROW), int(b.layout == ROW), M, N, K, float(alpha),
+              a.ptr, a.ld, _bstride(a, batch), b.ptr, b.ld, _bstride(b, batch), float(beta), db.ptr, db.ld,
+              _bstride(db, batch), *oa, *ob, *oc, batch, _stream())
+
+
+def trsm_bwd(uplo: int, unit: bool, A: torch.Tensor, X: torch.Tensor, Xbar: torch.Tensor, Bbar: torch.Tensor,
+             Abar=None) -> torch.Tensor:
+    """Adjoint of trsm(uplo, unit, A, B, X) (A*X = B, uplo of A as passed; a row-major A is
+    BLAST's trans() view): WRITES Bbar = A^{-T} Xbar (Bbar may be Xbar) and, if given,
+    ACCUMULATES -Bbar X^T on A's triangle (strictly, when unit) into Abar (A's shape and order)."""
+    a, x, xb = _as_mat(A, "A"), _as_mat(X, "X"), _as_mat(Xbar, "Xbar")
+    bb = _as_mat(Bbar, "Bbar")
+    m, n = x.rows, x.cols
+    if a.rows != m or a.cols != m or xb.rows != m or xb.cols != n or bb.rows != m or bb.cols != n:
+        raise ValueError("Invalid argument size")
+    for t, nm in ((x, "X"), (xb, "Xbar"), (bb, "Bbar")):
+        _square_col(t, nm)
+    batch = _batch_of(a, x, xb, bb)
+    if bb.batch != batch or (batch > 1 and bb.bstride == 0):
+        raise ValueError("Bbar must hold the whole batch")
+    oa = _out(Abar, "Abar", m, m, a.layout, batch)
+    _lib.call("blastgpu_dtrsm_bwd_strided", int(uplo), int(a.layout == ROW), int(bool(unit)), m, n, a.ptr, a.ld,
+              _bstride(a, batch), x.ptr, x.ld, _bstride(x, batch), xb.ptr, xb.ld, _bstride(xb, batch), bb.ptr, bb.ld,
+              bb.bstride, *oa, batch, _stream())
+    return Bbar
+
+
+def potrf_bwd(L: torch.Tensor, Lbar: torch.Tensor, Abar: torch.Tensor) -> torch.Tensor:
+    """Adjoint of L = chol(A) (potrf above): WRITES the symmetric dl/dA into Abar, in full, from L
+    and Lbar = dl/dL (lower triangles read)."""
+    lm, lb = _as_mat(L, "L"), _as_mat(Lbar, "Lbar")
+    n = lm.rows
+    if lm.cols != n or lb.rows != n or lb.cols != n:
+        raise ValueError("Invalid argument size")
+    _square_col(lm, "L")
+    _square_col(lb, "Lbar")
+    batch = _batch_of(lm, lb)
+    oa = _out(Abar, "Abar", n, n, COL, batch)
+    _lib.call("blastgpu_dpotrf_bwd_strided", n, lm.ptr, lm.ld, _bstride(lm, batch), lb.ptr, lb.ld,
+              _bstride(lb, batch), *oa, batch, _stream())
+    return Abar
+
+
 def _vec(v: torch.Tensor, name: str):
     """(batch, n) or (n,) float64 CUDA tensor -> (ptr, n, inc, batch, batch stride)."""
     if v.dtype != torch.float64 or not v.is_cuda:

@@ -357,6 +357,38 @@ typedef struct blastgpu_posv_bwd_desc {
 int blastgpu_dposv_bwd_batched(const blastgpu_posv_bwd_desc* desc, int64_t batch, int max_n,
                                int recompute, int32_t* info, blastgpu_stream_t stream);
 
+/* Adjoint of gemm D = alpha*op(A)*op(B) + beta*C (blastgpu_dgemm_strided's forward arguments):
+ * given Dbar = dl/dD (m x n), ACCUMULATES dl/dA into Abar (A's shape and orientation:
+ * m x k, or k x m when trans_a), dl/dB into Bbar (k x n, or n x k when trans_b) and dl/dC into
+ * Cbar (m x n): op(A)bar += alpha*Dbar*op(B)^T, op(B)bar += alpha*op(A)^T*Dbar,
+ * Cbar += beta*Dbar. Zero the outputs first for plain gradients. Abar, Bbar or Cbar may be null
+ * (not wanted). Uses blastgpu_dgemm_strided, so each product keeps its ascending-k order.
+ * For batch > 1 no output may have batch stride 0 (instances write concurrently). */
+int blastgpu_dgemm_bwd_strided(int trans_a, int trans_b, int m, int n, int k, double alpha, const double* A,
+                               int lda, int64_t stride_a, const double* B, int ldb, int64_t stride_b, double beta,
+                               const double* Dbar, int lddb, int64_t stride_db, double* Abar, int ldab,
+                               int64_t stride_ab, double* Bbar, int ldbb, int64_t stride_bb, double* Cbar, int ldcb,
+                               int64_t stride_cb, int64_t batch, blastgpu_stream_t stream);
+
+/* Adjoint of trsm op(A)*X = B (blastgpu_dtrsm_strided's forward arguments; uplo and unit describe
+ * op(A)): given the solution X and Xbar = dl/dX (m x n), WRITES Bbar = op(A)^{-T} Xbar (Bbar may
+ * equal Xbar) and, if Abar is not null, ACCUMULATES -Bbar*X^T on op(A)'s triangle (strictly
+ * below/above the diagonal when unit) into Abar in A's own orientation; Abar's other entries are
+ * not touched. Bbar must not alias X, A or Abar; for batch > 1 no output may have stride 0. */
+int blastgpu_dtrsm_bwd_strided(int uplo, int trans_a, int unit, int m, int n, const double* A, int lda,
+                               int64_t stride_a, const double* X, int ldx, int64_t stride_x, const double* Xbar,
+                               int ldxb, int64_t stride_xb, double* Bbar, int ldbb, int64_t stride_bb, double* Abar,
+                               int ldab, int64_t stride_ab, int64_t batch, blastgpu_stream_t stream);
+
+/* Adjoint of the Cholesky factorisation L = chol(A), lower (blastgpu_dpotrf_strided): given L and
+ * Lbar = dl/dL (lower triangles read), WRITES the symmetric gradient Abar = (S + S^T)/2 in full,
+ * S = L^{-T} Phi(L^T Lbar) L^{-1}, Phi = lower triangle with the diagonal halved (I. Murray,
+ * "Differentiation of the Cholesky decomposition", 2016); the convention of
+ * blastgpu_dposv_bwd_batched. Abar must not alias L or Lbar; for batch > 1 its stride is not 0. */
+int blastgpu_dpotrf_bwd_strided(int n, const double* L, int ldl, int64_t stride_l, const double* Lbar, int ldlb,
+                                int64_t stride_lb, double* Abar, int ldab, int64_t stride_ab, int64_t batch,
+                                blastgpu_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -147,3 +147,16 @@ def test_argument_validation_blas2_and_extensions(lib):
     assert call(a14=None) == -15  # the device workspace for L
     assert call(a15=None) == -16  # the device workspace for X
     assert call(a17=-1) == -18
+
+    # adjoints: invalid sizes, and a shared (stride 0) output for a batch of 2 (instances would race)
+    assert lib.blastgpu_dpotrf_bwd_strided(-1, p, 1, 0, p, 1, 0, p, 1, 0, 1, None) == -1
+    assert lib.blastgpu_dpotrf_bwd_strided(4, p, 3, 16, p, 4, 16, p, 4, 16, 1, None) == -3
+    assert lib.blastgpu_dpotrf_bwd_strided(4, p, 4, 16, p, 4, 16, p, 4, 0, 2, None) == -10
+    assert lib.blastgpu_dtrsm_bwd_strided(2, 0, 0, 4, 1, p, 4, 16, p, 4, 4, p, 4, 4, p, 4, 4, None, 4, 0, 1,
+                                          None) == -1
+    assert lib.blastgpu_dtrsm_bwd_strided(0, 0, 0, 4, 1, p, 4, 16, p, 4, 4, p, 4, 4, p, 4, 0, None, 4, 0, 2,
+                                          None) == -17
+    assert lib.blastgpu_dgemm_bwd_strided(0, 0, 2, 2, 2, 1.0, p, 2, 4, p, 2, 4, 1.0, p, 1, 4, None, 2, 0, None, 2,
+                                          0, None, 2, 0, 1, None) == -15
+    assert lib.blastgpu_dgemm_bwd_strided(0, 0, 2, 2, 2, 1.0, p, 2, 4, p, 2, 4, 1.0, p, 2, 4, p, 2, 0, None, 2, 0,
+                                          None, 2, 0, 2, None) == -19
