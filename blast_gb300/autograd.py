@@ -1,4 +1,5 @@
-"""torch.autograd shim over the batched Cholesky solve and its hand-written adjoint kernel.
+"""torch.autograd shims over the batched operations and their hand-written adjoints: the Cholesky
+solve (below), and gemm, trsm and potrf (at the end of this module).
 
 x = A^{-1} b for SPD A (binary64). Forward: potrf + potrs on the GPU (blastgpu_dposv_* entry
 points). Backward: blastgpu_dposv_bwd_batched, which returns dl/db = A^{-1} dl/dx and the
@@ -15,7 +16,7 @@ import numpy as np
 import torch
 
 from . import _lib, desc
-from .blast import col_major, posv
+from .blast import LOWER, col_major, gemm, gemm_bwd, posv, potrf, potrf_bwd, trsm, trsm_bwd
 
 
 def _colmajor_copy(t: torch.Tensor) -> torch.Tensor:
@@ -120,3 +121,91 @@ class PackedSPDSolve(torch.autograd.Function):
 
 def spd_solve_packed(A_flat, B_flat, ns, rs, keep_factor: bool = True) -> torch.Tensor:
     return PackedSPDSolve.apply(A_flat, B_flat, ns, rs, keep_factor)
+
+
+def _zeros_col(t: torch.Tensor) -> torch.Tensor:
+    return col_major(t.shape[:-2], t.shape[-2], t.shape[-1], t.device).zero_()
+
+
+class Gemm(torch.autograd.Function):
+    """D = alpha*A*B + beta*C (blast.gemm); backward: blastgpu_dgemm_bwd_strided."""
+
+    @staticmethod
+    def forward(ctx, A, B, C, alpha=1.0, beta=1.0):
+        Ac, Bc, Cc = _colmajor_copy(A), _colmajor_copy(B), _colmajor_copy(C)
+        D = col_major(C.shape[:-2], C.shape[-2], C.shape[-1], C.device)
+        gemm(float(alpha), Ac, Bc, float(beta), Cc, D)
+        ctx.save_for_backward(Ac, Bc)
+        ctx.alpha, ctx.beta = float(alpha), float(beta)
+        return D.clone()
+
+    @staticmethod
+    def backward(ctx, Dbar):
+        Ac, Bc = ctx.saved_tensors
+        G = _colmajor_copy(Dbar)
+        need = ctx.needs_input_grad
+        GA = _zeros_col(Ac) if need[0] else None
+        GB = _zeros_col(Bc) if need[1] else None
+        GC = _zeros_col(G) if need[2] else None
+        gemm_bwd(ctx.alpha, Ac, Bc, ctx.beta, G, GA, GB, GC)
+        return GA, GB, GC, None, None
+
+
+class Trsm(torch.autograd.Function):
+    """X = A^{-1} B, A triangular (blast.trsm: uplo, unit diagonal); backward:
+    blastgpu_dtrsm_bwd_strided. Entries of A outside its triangle (and a unit diagonal) are not
+    read, and their gradient is zero."""
+
+    @staticmethod
+    def forward(ctx, A, B, uplo=LOWER, unit=False):
+        Ac, Bc = _colmajor_copy(A), _colmajor_copy(B)
+        X = col_major(B.shape[:-2], B.shape[-2], B.shape[-1], B.device)
+        trsm(int(uplo), bool(unit), Ac, Bc, X)
+        ctx.save_for_backward(Ac, X)
+        ctx.uplo, ctx.unit = int(uplo), bool(unit)
+        return X.clone()
+
+    @staticmethod
+    def backward(ctx, Xbar):
+        Ac, X = ctx.saved_tensors
+        G = _colmajor_copy(Xbar)
+        GB = _zeros_col(X)
+        GA = _zeros_col(Ac) if ctx.needs_input_grad[0] else None
+        trsm_bwd(ctx.uplo, ctx.unit, Ac, X, G, GB, GA)
+        return GA, GB if ctx.needs_input_grad[1] else None, None, None
+
+
+class Potrf(torch.autograd.Function):
+    """L = chol(A), lower, strictly upper part zero (blast.potrf reads the lower triangle of A);
+    backward: blastgpu_dpotrf_bwd_strided, the symmetric dl/dA (as for the solve above)."""
+
+    @staticmethod
+    def forward(ctx, A):
+        Ac = _colmajor_copy(A)
+        L = _zeros_col(Ac)
+        potrf(Ac, L)
+        ctx.save_for_backward(L)
+        return L.clone()
+
+    @staticmethod
+    def backward(ctx, Lbar):
+        (L,) = ctx.saved_tensors
+        G = _colmajor_copy(Lbar)
+        GA = col_major(L.shape[:-2], L.shape[-2], L.shape[-1], L.device)
+        potrf_bwd(L, G, GA)
+        return GA.clone()
+
+
+def gemm_fn(A, B, C, alpha=1.0, beta=1.0) -> torch.Tensor:
+    """Differentiable D = alpha*A*B + beta*C (binary64, CUDA)."""
+    return Gemm.apply(A, B, C, alpha, beta)
+
+
+def trsm_fn(A, B, uplo=LOWER, unit=False) -> torch.Tensor:
+    """Differentiable X = A^{-1} B for triangular A (binary64, CUDA)."""
+    return Trsm.apply(A, B, uplo, unit)
+
+
+def potrf_fn(A) -> torch.Tensor:
+    """Differentiable lower Cholesky factor (binary64, CUDA)."""
+    return Potrf.apply(A)
