@@ -160,3 +160,35 @@ def test_argument_validation_blas2_and_extensions(lib):
                                           0, None, 2, 0, 1, None) == -15
     assert lib.blastgpu_dgemm_bwd_strided(0, 0, 2, 2, 2, 1.0, p, 2, 4, p, 2, 4, 1.0, p, 2, 4, p, 2, 0, None, 2, 0,
                                           None, 2, 0, 2, None) == -19
+
+
+def test_descriptor_layouts_match_header(tmp_path):
+    """The numpy descriptor dtypes of blast_gb300.desc have exactly the byte layout of the C
+    structs in include/blastgpu.h (sizes and field offsets, as a C compiler lays them out)."""
+    from blast_gb300 import desc
+
+    structs = {
+        "blastgpu_mat": (desc.MAT_DTYPE, ["data", "rows", "cols", "ld", "layout", "ps", "reserved"]),
+        "blastgpu_gemm_desc": (desc.GEMM_DTYPE, ["A", "B", "C", "D", "alpha", "beta"]),
+        "blastgpu_getrf_desc": (desc.GETRF_DTYPE, ["A", "ipiv", "B"]),
+        "blastgpu_posv_desc": (desc.POSV_DTYPE, ["A", "L", "B", "X", "ws_offset"]),
+        "blastgpu_posv_bwd_desc": (desc.POSV_BWD_DTYPE, ["A", "L", "X", "Xbar", "Bbar", "Abar"]),
+        "blastgpu_potrf_desc": (desc.POTRF_DTYPE, ["A", "L"]),
+        "blastgpu_copy_desc": (desc.COPY_DTYPE, ["src", "dst"]),
+    }
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "blastgpu.h"', "int main(void) {"]
+    for name, (_, fields) in structs.items():
+        lines.append(f'    printf("{name} %zu\\n", sizeof({name}));')
+        for f in fields:
+            lines.append(f'    printf("{name}.{f} %zu\\n", offsetof({name}, {f}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                           check=True).stdout.splitlines())
+    for name, (dt, fields) in structs.items():
+        assert int(got[name]) == dt.itemsize, name
+        for f in fields:
+            assert int(got[f"{name}.{f}"]) == dt.fields[f][1], (name, f)
