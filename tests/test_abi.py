@@ -192,3 +192,22 @@ def test_descriptor_layouts_match_header(tmp_path):
         assert int(got[name]) == dt.itemsize, name
         for f in fields:
             assert int(got[f"{name}.{f}"]) == dt.fields[f][1], (name, f)
+
+
+def test_cpp_shim_compiles_and_links(lib, tmp_path):
+    """include/blastgpu/blast.hpp (BLAST's names over the C ABI) and the example program that uses
+    it compile with the host C++ compiler and link against the library (running it needs a GPU:
+    tests/test_gpu_cpp_shim.py)."""
+    import os
+    import shutil
+
+    cuda = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None or not (cuda / "include" / "cuda_runtime.h").exists():
+        pytest.skip("no host C++ compiler or CUDA headers")
+    libpath = Path(lib._name)
+    exe = tmp_path / "test_shim"
+    subprocess.run([cxx, "-std=c++17", "-Wall", str(ROOT / "tests" / "cpp" / "test_shim.cpp"), "-I",
+                    str(ROOT / "include"), "-I", str(cuda / "include"), "-L", str(libpath.parent), "-lblastgpu", "-L",
+                    str(cuda / "lib64"), "-lcudart", "-o", str(exe)], check=True)
+    assert exe.exists()
