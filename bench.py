@@ -275,7 +275,8 @@ def run_reference(args):
             "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "impl": "reference",
-            "config": {"workload": WORKLOAD, "batch": BATCH, "n": N, "nrhs": NRHS},
+            "config": {"workload": WORKLOAD, "batch_per_gpu": BATCH, "n": N, "nrhs": NRHS,
+                       "parallelism": f"host cores of rank 0 ({threads} threads)"},
             "gflops": rate * FLOPS_PER / 1e9,
             "cpu_baseline": {"value": rate, "unit": "matrices/s", "cores": threads, "kind": "port",
                              "sample": f"{args.steps} timed passes over {BATCH} matrices after "

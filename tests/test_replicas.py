@@ -69,3 +69,24 @@ def test_gloo_world2_replicas(tmp_path):
     ns = np.random.default_rng(7).integers(4, 40, 37)
     expect = np.array([1 if i % 9 == 0 else 0 for i in range(len(ns))], dtype=np.int32)
     assert np.array_equal(full, expect)
+
+
+def test_bench_reference_arm_under_torchrun(tmp_path):
+    """`bench.py --impl reference` launched like the N-GPU bench (torch.distributed.run, two ranks):
+    rank 0 alone times the CPU restatement and prints one JSON line; the other rank exits 0."""
+    import json
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parent.parent
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), str(root / "bench.py"),
+           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "1"]
+    out = subprocess.run(cmd, cwd=root, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [json.loads(x) for x in out.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1
+    line = lines[0]
+    assert line["impl"] == "reference" and line["unit"] == "matrices/s" and line["value"] > 0
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
