@@ -213,6 +213,22 @@ def gemm_batch(alpha, A, B, beta, C, threads: int = 0):
     return _from_batch(D, m, n)
 
 
+def gemm_prepare(alpha, A, B, beta, C) -> dict:
+    """Column-major flat buffers of a uniform gemm batch for repeated timed runs of gemm_run."""
+    batch, m, k = A.shape
+    n = B.shape[2]
+    a, b, c = (_batch_colmajor(x) for x in (A, B, C))
+    return {"m": m, "n": n, "k": k, "alpha": alpha, "beta": beta, "batch": batch, "A": a, "B": b, "C": c,
+            "D": np.empty_like(c)}
+
+
+def gemm_run(p: dict, threads: int = 0) -> None:
+    m, n, k = p["m"], p["n"], p["k"]
+    lib().oracle_dgemm_batch(m, n, k, p["alpha"], p["A"].ctypes.data, m * k, p["B"].ctypes.data, k * n,
+                             p["beta"], p["C"].ctypes.data, m * n, p["D"].ctypes.data, m * n, p["batch"],
+                             threads)
+
+
 def _batch_colmajor(x: np.ndarray) -> np.ndarray:
     """(batch, r, c) -> flat buffer holding each matrix column-major, contiguous per instance."""
     return np.ascontiguousarray(np.swapaxes(x, 1, 2)).reshape(-1)

@@ -90,3 +90,8 @@ def test_bench_reference_arm_under_torchrun(tmp_path):
     line = lines[0]
     assert line["impl"] == "reference" and line["unit"] == "matrices/s" and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+    # the workload-defining keys are the ones the GPU arm prints (bench.contract_config)
+    sys.path.insert(0, str(root))
+    import bench
+
+    assert line["config"] == bench.contract_config()
