@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "../../include/blastgpu.h"
 
 namespace blastgpu {
@@ -27,6 +29,25 @@ inline cudaStream_t as_cuda(blastgpu_stream_t s) { return reinterpret_cast<cudaS
 
 // Number of SMs of the current device (cached per device).
 int sm_count();
+
+// Raises Kernel's dynamic shared-memory limit to at least `bytes` on the current device. The
+// attribute belongs to the (kernel, device) pair, so the flag is kept per device: a call on a
+// second GPU of the same process sets it there too. Setting it is not a stream operation, so a
+// launch captured into a CUDA graph after the first call on that device replays with it set.
+constexpr int kMaxDevices = 64;
+template <auto Kernel>
+cudaError_t ensure_smem(size_t bytes) {
+    static std::atomic<size_t> done[kMaxDevices];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices)
+        return cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (done[dev].load(std::memory_order_acquire) >= bytes) return cudaSuccess;
+    e = cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) done[dev].store(bytes, std::memory_order_release);
+    return e;
+}
 
 // D_lower = beta*C + alpha*op(A)*op(A)^T on a uniform batch, syrkLower's order (blas3.cu);
 // op(A) = A (m x k) or, with trans_a, the transpose of a k x m A.

@@ -475,12 +475,9 @@ int launch_getrs(Batch const& batch, int64_t count, int max_n, const int32_t* in
     if (blocks > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
     size_t const smem = sizeof(double) * 32 * (size_t)max_n;
     if (smem > 200 * 1024) return BLASTGPU_ERR_TOO_LARGE;
-    static std::atomic<size_t> smem_set{0};
-    if (smem > 48 * 1024 && smem_set.load() < smem) {
-        cudaError_t const e =
-            cudaFuncSetAttribute(getrs_kernel<Batch>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (smem > 48 * 1024) {
+        cudaError_t const e = ensure_smem<getrs_kernel<Batch>>(200 * 1024);
         if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
-        smem_set.store(200 * 1024);
     }
     getrs_kernel<Batch><<<(unsigned)blocks, 32, smem, s>>>(batch, count, info);
     return check_launch();

@@ -54,13 +54,22 @@ struct CtaItem {
     char* ws;                 // per-instance workspace (mixed path)
 };
 
+// capacity > 0: the workspace is a fixed array of that many bytes (the allocation-free entry
+// point); an instance whose scratch range [ws_offset, ws_offset + n*n*4) is not inside it, or whose
+// offset is not 4-byte aligned, comes back with n = -1 and is not solved.
 struct DescPosv {
     const blastgpu_posv_desc* desc;
     char* workspace;
+    int64_t capacity = 0;
     __device__ CtaItem get(int64_t b) const {
         blastgpu_posv_desc const& d = desc[b];
-        return {d.A.rows, d.A.data, d.A.ld, d.L.data, d.L.ld, d.B.data, d.B.ld,
-                d.X.data, d.X.ld, d.B.cols, workspace ? workspace + d.ws_offset : nullptr};
+        int n = d.A.rows;
+        if (capacity > 0) {
+            int64_t const need = (int64_t)sizeof(float) * n * n;
+            if (d.ws_offset < 0 || (d.ws_offset & 3) != 0 || d.ws_offset > capacity - need) n = -1;
+        }
+        return {n, d.A.data, d.A.ld, d.L.data, d.L.ld, d.B.data, d.B.ld,
+                d.X.data, d.X.ld, d.B.cols, workspace && n >= 0 ? workspace + d.ws_offset : nullptr};
     }
 };
 
@@ -630,6 +639,14 @@ __global__ void __launch_bounds__(kThreads, 2) posv_cta_mixed_kernel(Batch batch
     if (b >= args.batch) return;
     CtaItem const it = batch.get(b);
     int const n = it.n, tid = threadIdx.x;
+    if (n < 0) {  // scratch range outside the fixed array: reported, nothing written
+        if (tid == 0) {
+            if (args.info) args.info[b] = -1;
+            if (args.iters) args.iters[b] = 0;
+            if (args.berr) args.berr[b] = CUDART_NAN;
+        }
+        return;
+    }
     float* F = reinterpret_cast<float*>(it.ws);
     for (int i = tid; i < n; i += kThreads) r[i] = 0.0;
     __syncthreads();
@@ -772,18 +789,6 @@ __global__ void __launch_bounds__(kThreads, MAXR <= 4 ? 2 : 1)
         }
 }
 
-// Raises a kernel's dynamic shared-memory limit once per process (before any stream capture
-// that replays the launch, the attribute is already set; setting it is not a stream operation).
-// The template parameter is the kernel itself, so every kernel has its own flag.
-template <auto Kernel>
-cudaError_t ensure_smem(size_t bytes) {
-    static std::atomic<size_t> done{0};
-    if (done.load(std::memory_order_acquire) >= bytes) return cudaSuccess;
-    cudaError_t const e = cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e == cudaSuccess) done.store(bytes, std::memory_order_release);
-    return e;
-}
-
 template <int MAXR>
 int launch_bwd(DescBwd const& batch, int64_t count, int recompute, int32_t* info, cudaStream_t s) {
     size_t const smem = Smem<double, MAXR>::kBytes;
@@ -867,7 +872,8 @@ int blastgpu_dposv_mixed_batched_noalloc(const blastgpu_posv_desc* desc, int64_t
     cudaError_t const e = noalloc_scratch(&scratch);
     if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
     CtaArgs a{batch, info, iters, berr, tol, max_iter};
-    return dispatch_cta(true, max_n, DescPosv{desc, static_cast<char*>(scratch)}, a, as_cuda(stream));
+    return dispatch_cta(true, max_n, DescPosv{desc, static_cast<char*>(scratch), (int64_t)kNoAllocScratchBytes}, a,
+                        as_cuda(stream));
 }
 
 size_t blastgpu_dposv_mixed_workspace_bytes(int n) {

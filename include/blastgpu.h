@@ -89,6 +89,9 @@ int blastgpu_tune_get(const char* key, int* value);
  * measures the device's binary64 FMA throughput (TFLOP/s) on `stream` and synchronises it. */
 int blastgpu_selftest_recip(int which, const double* x, double* y, int n, blastgpu_stream_t stream);
 int blastgpu_probe_fp64_tflops(double* tflops, blastgpu_stream_t stream);
+/* probe_fp64_dmma_tflops: the same measurement for the binary64 tensor-core instruction
+ * (mma.sync m8n8k4 f64), so that its rate can be compared with the FMA pipe's on the same GPU. */
+int blastgpu_probe_fp64_dmma_tflops(double* tflops, blastgpu_stream_t stream);
 
 /* blastgpu_dposv_strided for operands outside device memory: A and B are read in place and L and
  * X written in place, each element once, from/to any memory the GPU can address (pinned host
@@ -328,8 +331,14 @@ int blastgpu_dposv_mixed_batched(const blastgpu_posv_desc* desc, int64_t batch, 
  *   - scratch_bytes states the bytes the descriptors' ws_offset ranges use (max over instances
  *     of ws_offset + blastgpu_dposv_mixed_workspace_bytes(n)); larger than the capacity returns
  *     BLASTGPU_ERR_TOO_LARGE and launches nothing;
+ *   - the kernel checks every descriptor's range [ws_offset, ws_offset + 4*n*n) against the
+ *     capacity as well: an instance whose range is not inside the array (or whose ws_offset is
+ *     not a multiple of 4) is not solved and gets info = -1, iters = 0, berr = NaN, while the
+ *     other instances of the batch are solved normally;
  *   - the first call on a device looks up the array's device address (cudaGetSymbolAddress) and
- *     caches it; make that first call before any stream capture;
+ *     caches it; make that first call before any stream capture. cudaDeviceReset unloads the
+ *     library's device code and so invalidates the cached address: after a reset, do not call
+ *     this entry point again in the same process;
  *   - every call reuses the same array (nothing in it needs clearing: each factor is written
  *     before it is read), so calls whose kernels overlap on the GPU race: serialise them.
  * No cudaMalloc, cudaFree or allocating library routine is called. Results equal

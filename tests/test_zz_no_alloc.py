@@ -80,6 +80,29 @@ def test_noalloc_matches_workspace_entry_point(gpu):
         for n, xr, xn in zip(ns, x_ref, X_na.to_list()):
             assert normwise(xn, xr) <= 1e-12, (call, n)
 
+    # a descriptor whose scratch range runs past the array (a miscounted scratch_bytes) is not
+    # solved and reports info = -1; the other instances of the same batch are unaffected
+    recs = np.zeros(count, dtype=desc.POSV_DTYPE)
+    bad = 3
+    for i in range(count):
+        off = int(offs[i])
+        if i == bad:
+            off = _lib.NOALLOC_SCRATCH_BYTES - int(per[i]) + 256
+        recs[i] = (A.record(i), desc.EMPTY_MAT, B.record(i), X_na.record(i), off)
+    d_bad = desc.upload(recs, "cuda")
+    X_na.buf.fill_(7.0)
+    infos[1].fill_(-9)
+    _lib.call("blastgpu_dposv_mixed_batched_noalloc", d_bad.data_ptr(), count, max_n, scratch_bytes,
+              1e-12, 10, infos[1].data_ptr(), outs[1].data_ptr(), berrs[1].data_ptr(), stream)
+    torch.cuda.synchronize()
+    info_h, berr_h = infos[1].cpu().numpy(), berrs[1].cpu().numpy()
+    assert info_h[bad] == -1 and np.isnan(berr_h[bad])
+    assert np.all(X_na.to_list()[bad] == 7.0)  # nothing written for the refused instance
+    for i, (n, xr, xn) in enumerate(zip(ns, x_ref, X_na.to_list())):
+        if i != bad:
+            assert info_h[i] == 0 and berr_h[i] <= 1e-12
+            assert normwise(xn, xr) <= 1e-12, (i, n)
+
     # a batch that needs more scratch than the array holds is refused before any launch
     launches = _lib.launch_count()
     st = _lib.lib().blastgpu_dposv_mixed_batched_noalloc(
