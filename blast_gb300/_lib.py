@@ -90,6 +90,17 @@ SIGNATURES: dict[str, list] = {
     "blastgpu_dposv_mixed_batched": [PTR, I64, I32, PTR, DBL, I32, PTR, PTR, PTR, PTR],
     "blastgpu_dposv_bwd_batched": [PTR, I64, I32, I32, PTR, PTR],
     "blastgpu_dposv_mixed_batched_noalloc": [PTR, I64, I32, C.c_size_t, DBL, I32, PTR, PTR, PTR, PTR],
+    "blastgpu_dpotrf_mn_strided": [I32, I32, PTR, I32, I64, PTR, I32, I64, PTR, I64, PTR],
+    "blastgpu_dsyrk_lower_batched": [PTR, I64, PTR, PTR],
+    "blastgpu_dtrsm_batched": [I32, I32, I32, PTR, I64, PTR, PTR],
+    "blastgpu_dtrmm_batched": [I32, I32, I32, PTR, I64, PTR, PTR],
+    "blastgpu_dger_batched": [PTR, I64, PTR, PTR],
+    "blastgpu_idamax_batched": [PTR, I64, PTR, PTR],
+    "blastgpu_dlaswp_batched": [PTR, I64, PTR, PTR],
+    "blastgpu_dswap_batched": [PTR, I64, PTR, PTR],
+    "blastgpu_dgemm_bwd_batched": [PTR, I64, I32, PTR, PTR],
+    "blastgpu_dtrsm_bwd_batched": [I32, I32, PTR, I64, PTR, PTR],
+    "blastgpu_dpotrf_bwd_batched": [PTR, I64, PTR, PTR],
 }
 _RESTYPES = {"blastgpu_status_string": C.c_char_p, "blastgpu_launch_count": C.c_int64,
              "blastgpu_dposv_mixed_workspace_bytes": C.c_size_t}

@@ -113,22 +113,25 @@ def _info_tensor(batch: int, device) -> torch.Tensor:
 def potrf(A: torch.Tensor, L: torch.Tensor) -> torch.Tensor:
     """Lower Cholesky factor: L := chol(A)  (blast::potrf, dense/Potrf.hpp:66-106).
 
-    Reads the lower triangle of A; writes the lower triangle of L (L may be A). Returns the
-    per-instance info (0, or j+1 for the first non-positive pivot).
+    Reads the lower triangle of A; writes the lower triangle of L (L may be A). A may be an
+    M x N trapezoid with M >= N, as in BLAST (the rows below the top N x N block are solved against
+    its factor). Returns the per-instance info (0, or j+1 for the first non-positive pivot).
     """
     a, l = _as_mat(A, "A"), _as_mat(L, "L")
     if a.cols > a.rows:
         raise ValueError("Invalid matrix size")
     if l.rows != a.rows or l.cols != a.cols:
         raise ValueError("Invalid matrix size")
-    if a.rows != a.cols:
-        raise NotImplementedError("trapezoidal potrf (M > N) is not exposed by the batched ABI")
     _square_col(a, "A")
     _square_col(l, "L")
     batch = _batch_of(a, l)
     info = _info_tensor(batch, A.device)
-    _lib.call("blastgpu_dpotrf_strided", a.rows, a.ptr, a.ld, _bstride(a, batch), l.ptr, l.ld,
-              l.bstride, info.data_ptr(), batch, _stream())
+    if a.rows == a.cols:
+        _lib.call("blastgpu_dpotrf_strided", a.rows, a.ptr, a.ld, _bstride(a, batch), l.ptr, l.ld,
+                  l.bstride, info.data_ptr(), batch, _stream())
+    else:
+        _lib.call("blastgpu_dpotrf_mn_strided", a.rows, a.cols, a.ptr, a.ld, _bstride(a, batch), l.ptr,
+                  l.ld, l.bstride, info.data_ptr(), batch, _stream())
     return info
 
 

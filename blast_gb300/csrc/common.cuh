@@ -55,6 +55,12 @@ int launch_syrk_lower(int m, int k, int trans_a, double alpha, const double* A, 
                       double beta, const double* C, int ldc, int64_t sc, double* D, int ldd, int64_t sd,
                       int64_t batch, cudaStream_t s);
 
+// Uniform batch of Cholesky solves (or factorisations: nrhs = 0; or solves with a given factor:
+// A = nullptr) on the CTA-per-matrix kernels of posv_cta.cu, n <= 512. L may equal A, X may equal B.
+int launch_posv_cta_strided(int n, int nrhs, const double* A, int lda, int64_t sa, double* L, int ldl,
+                            int64_t sl, const double* B, int ldb, int64_t sb, double* X, int ldx, int64_t sx,
+                            int32_t* info, int64_t batch, cudaStream_t s);
+
 // Kernel-selection parameters set by the autotuner (blastgpu_tune_set); `fallback` if unset.
 int tune_get(const char* key, int fallback);
 
@@ -87,6 +93,31 @@ struct MatView {
 
 __device__ __forceinline__ MatView view(blastgpu_mat const& m) {
     return MatView{m.data, m.ld, m.layout, m.ps > 0 ? m.ps : 1};
+}
+
+// Device-side validation of a view read from a descriptor (the host cannot read device-resident
+// descriptors): extents, a data pointer, and a leading dimension that covers the extents.
+__device__ __forceinline__ bool view_ok(blastgpu_mat const& m) {
+    if (m.rows < 0 || m.cols < 0) return false;
+    if (m.rows == 0 || m.cols == 0) return true;
+    if (m.data == nullptr) return false;
+    switch (m.layout) {
+        case BLASTGPU_COL_MAJOR: return m.ld >= m.rows;
+        case BLASTGPU_ROW_MAJOR: return m.ld >= m.cols;
+        case BLASTGPU_PANEL: return m.ps > 0 && (int64_t)m.ld >= (int64_t)m.ps * m.cols;
+        default: return false;
+    }
+}
+
+// The transpose of a dense view (column-major <-> row-major over the same storage, BLAST's
+// trans()); panel storage has no transposed view (returns false).
+__device__ __forceinline__ bool transposed(blastgpu_mat const& m, blastgpu_mat& t) {
+    if (m.layout == BLASTGPU_PANEL) return false;
+    t = m;
+    t.rows = m.cols;
+    t.cols = m.rows;
+    t.layout = m.layout == BLASTGPU_COL_MAJOR ? BLASTGPU_ROW_MAJOR : BLASTGPU_COL_MAJOR;
+    return true;
 }
 
 // Host-side validation of one descriptor.

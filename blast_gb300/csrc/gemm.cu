@@ -48,6 +48,66 @@ struct DescGemm {
     }
 };
 
+// Adjoint of D = alpha*A*B + beta*C over descriptors (A, B as views, so op() is the view):
+// which = 0 forms Abar += alpha*Dbar*B^T in A's orientation, which = 1 forms Bbar += alpha*A^T*Dbar
+// in B's; both are gemms with beta = 1 on transposed views, in place. An instance whose shapes
+// do not fit (gemm_bwd_ok) or whose gradient is not wanted (null data) gets m = 0.
+__device__ __forceinline__ bool gemm_bwd_ok(blastgpu_gemm_bwd_desc const& g) {
+    int const m = g.Dbar.rows, n = g.Dbar.cols, k = g.A.cols;
+    blastgpu_mat t;
+    if (!view_ok(g.Dbar) || g.A.rows != m || g.B.rows != k || g.B.cols != n) return false;
+    if (g.Abar.data && !(view_ok(g.B) && transposed(g.B, t) && view_ok(g.Abar) && g.Abar.rows == m && g.Abar.cols == k))
+        return false;
+    if (g.Bbar.data && !(view_ok(g.A) && transposed(g.A, t) && view_ok(g.Bbar) && g.Bbar.rows == k && g.Bbar.cols == n))
+        return false;
+    if (g.Cbar.data && !(view_ok(g.Cbar) && g.Cbar.rows == m && g.Cbar.cols == n)) return false;
+    return true;
+}
+
+struct GemmBwdBatch {
+    const blastgpu_gemm_bwd_desc* desc;
+    int which;
+    __device__ void get(int64_t b, int& mm, int& nn, int& kk, double& al, double& be, MatView& a, MatView& bm,
+                        MatView& c, MatView& d) const {
+        blastgpu_gemm_bwd_desc const& g = desc[b];
+        mm = nn = kk = 0;
+        al = g.alpha;
+        be = 1.0;
+        if (!gemm_bwd_ok(g)) return;
+        blastgpu_mat t;
+        if (which == 0) {
+            if (!g.Abar.data) return;
+            transposed(g.B, t);
+            mm = g.Abar.rows; nn = g.Abar.cols; kk = g.Dbar.cols;
+            a = view(g.Dbar); bm = view(t); c = view(g.Abar);
+        } else {
+            if (!g.Bbar.data) return;
+            transposed(g.A, t);
+            mm = g.Bbar.rows; nn = g.Bbar.cols; kk = g.Dbar.rows;
+            a = view(t); bm = view(g.Dbar); c = view(g.Bbar);
+        }
+        d = c;
+    }
+};
+
+// Cbar += beta*Dbar (fma(beta, dbar, cbar), as the strided adjoint) and the status of every instance.
+__global__ void __launch_bounds__(128) gemm_bwd_c_kernel(const blastgpu_gemm_bwd_desc* desc, int64_t count,
+                                                         int32_t* status) {
+    int64_t const b = (int64_t)blockIdx.x * 4 + (threadIdx.x >> 5);
+    int const lane = threadIdx.x & 31;
+    if (b >= count) return;
+    blastgpu_gemm_bwd_desc const& g = desc[b];
+    bool const ok = gemm_bwd_ok(g);
+    if (status && lane == 0) status[b] = ok ? 0 : -1;
+    if (!ok || !g.Cbar.data) return;
+    MatView const Db = view(g.Dbar), Cb = view(g.Cbar);
+    int const m = g.Dbar.rows, n = g.Dbar.cols;
+    for (int e = lane; e < m * n; e += 32) {
+        int const i = e % m, j = e / m;
+        Cb(i, j) = fma(g.beta, Db(i, j), Cb(i, j));
+    }
+}
+
 template <int RM, int RN, class Batch>
 __global__ void __launch_bounds__(kWarps * 32) gemm_warp_kernel(Batch batch, int64_t count) {
     constexpr int WM = 4 * RM, WN = 8 * RN;
@@ -177,6 +237,23 @@ int blastgpu_dgemm_strided(int trans_a, int trans_b, int m, int n, int k, double
     g.D = MatView{D, ldd, BLASTGPU_COL_MAJOR, 1};
     g.sa = stride_a; g.sb = stride_b; g.sc = stride_c; g.sd = stride_d;
     return launch_gemm(g, batch, m, n, as_cuda(stream));
+}
+
+int blastgpu_dgemm_bwd_batched(const blastgpu_gemm_bwd_desc* desc, int64_t batch, int max_dim, int32_t* status,
+                               blastgpu_stream_t stream) {
+    if (batch < 0) return -2;
+    if (batch == 0) return BLASTGPU_SUCCESS;
+    if (!desc) return -1;
+    if (max_dim < 0) return -3;
+    int64_t const blocks = (batch + 3) / 4;
+    if (blocks > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
+    cudaStream_t const s = as_cuda(stream);
+    gemm_bwd_c_kernel<<<(unsigned)blocks, 128, 0, s>>>(desc, batch, status);
+    int st = check_launch();
+    if (st != BLASTGPU_SUCCESS) return st;
+    st = launch_gemm(GemmBwdBatch{desc, 0}, batch, max_dim, max_dim, s);
+    if (st != BLASTGPU_SUCCESS) return st;
+    return launch_gemm(GemmBwdBatch{desc, 1}, batch, max_dim, max_dim, s);
 }
 
 int blastgpu_dgemm_batched(const blastgpu_gemm_desc* desc, int64_t batch, int max_m, int max_n,

@@ -54,6 +54,19 @@ struct CtaItem {
     char* ws;                 // per-instance workspace (mixed path)
 };
 
+// Uniform batch: instance b at base + b * stride (A = nullptr: solves only, with the given L).
+struct StridedPosv {
+    int n, nrhs;
+    const double* A; int lda; int64_t sa;
+    double* L; int ldl; int64_t sl;
+    const double* B; int ldb; int64_t sb;
+    double* X; int ldx; int64_t sx;
+    __device__ CtaItem get(int64_t b) const {
+        return {n, A ? A + b * sa : nullptr, lda, L + b * sl, ldl, nrhs ? B + b * sb : nullptr, ldb,
+                nrhs ? X + b * sx : nullptr, ldx, nrhs, nullptr};
+    }
+};
+
 // capacity > 0: the workspace is a fixed array of that many bytes (the allocation-free entry
 // point); an instance whose scratch range [ws_offset, ws_offset + n*n*4) is not inside it, or whose
 // offset is not 4-byte aligned, comes back with n = -1 and is not solved.
@@ -611,8 +624,10 @@ __global__ void __launch_bounds__(kThreads, MAXR <= 8 ? 2 : 1) posv_cta_f64_kern
     if (b >= args.batch) return;
     CtaItem const it = batch.get(b);
     int const n = it.n;
-    int const info = cta_potrf<double, MAXR>(n, it.A, it.lda, it.L, it.ldl, buf, &s_info);
-    if (threadIdx.x == 0 && args.info) args.info[b] = info;
+    if (it.A != nullptr) {  // A == nullptr: solves with the given factor L only
+        int const info = cta_potrf<double, MAXR>(n, it.A, it.lda, it.L, it.ldl, buf, &s_info);
+        if (threadIdx.x == 0 && args.info) args.info[b] = info;
+    }
     for (int c = 0; c < it.nrhs; ++c) {
         for (int i = threadIdx.x; i < n; i += kThreads) vec[i] = it.B[i + (int64_t)c * it.ldb];
         __syncthreads();
@@ -823,6 +838,18 @@ int dispatch_cta(bool mixed, int max_n, Batch const& batch, CtaArgs const& args,
     if (max_n <= 512) return launch_cta<16>(mixed, batch, args, s);
     return BLASTGPU_ERR_TOO_LARGE;
 }
+
+}  // namespace
+
+int launch_posv_cta_strided(int n, int nrhs, const double* A, int lda, int64_t sa, double* L, int ldl,
+                            int64_t sl, const double* B, int ldb, int64_t sb, double* X, int ldx, int64_t sx,
+                            int32_t* info, int64_t batch, cudaStream_t s) {
+    StridedPosv const p{n, nrhs, A, lda, sa, L, ldl, sl, B, ldb, sb, X, ldx, sx};
+    CtaArgs const a{batch, info, nullptr, nullptr, 0.0, 0};
+    return dispatch_cta(false, n, p, a, s);
+}
+
+namespace {
 
 // Scratch for blastgpu_dposv_mixed_batched_noalloc: a fixed array in the module's device memory,
 // reserved on every GPU that loads the library until the process exits. It holds the binary32

@@ -96,10 +96,14 @@ struct SyrkSrc {
     }
 };
 
-// One KM x KN register tile of the left-looking strip k (rows i .. i+KM-1). DIAG: the strip's
+// One KM x KN register tile of the left-looking strip k (rows i .. i+KM-1 of the n rows passed
+// as the first argument, the matrix's row count). DIAG: the strip's
 // first tile, which holds the diagonal block; its strictly upper entries (r < c) are never stored,
 // so their fused multiply-adds are left out at compile time.
-template <int KM, int KN, bool DIAG, class Src, class Addr>
+// PF: the operands of column l + 1 are loaded before the fused multiply-adds of column l (one column
+// of look-ahead), so that a load's latency overlaps the previous column's arithmetic; the order of
+// operations on every element is the same either way.
+template <int KM, int KN, bool DIAG, bool PF = false, class Src, class Addr>
 __device__ __forceinline__ void potrf_tile(int n, int k, int i, int nc, Src const& src, double* L, Addr il,
                                            double (&y)[KN], int& info) {
     constexpr bool diag = DIAG;
@@ -108,17 +112,44 @@ __device__ __forceinline__ void potrf_tile(int n, int k, int i, int nc, Src cons
 
     // acc -= L(i:i+KM, 0:k) * L(k:k+KN, 0:k)^T, one fused rank-1 update per column l
     // (BLAST's ger(-1, ...) loop, dense/Potrf.hpp:40-41).
-    for (int l = 0; l < k; ++l) {
+    if constexpr (PF) {
         double a[KM], b[KN];
+        if (k > 0) {
 #pragma unroll
-        for (int r = 0; r < KM; ++r) a[r] = (i + r < n) ? L[il(i + r, l)] : 0.0;
+            for (int r = 0; r < KM; ++r) a[r] = (i + r < n) ? L[il(i + r, 0)] : 0.0;
 #pragma unroll
-        for (int c = 0; c < KN; ++c) b[c] = (c < nc) ? L[il(k + c, l)] : 0.0;
+            for (int c = 0; c < KN; ++c) b[c] = (c < nc) ? L[il(k + c, 0)] : 0.0;
+        }
+        for (int l = 0; l < k; ++l) {
+            double an[KM], bn[KN];
+            int const ln = l + 1 < k ? l + 1 : l;
 #pragma unroll
-        for (int c = 0; c < KN; ++c)
+            for (int r = 0; r < KM; ++r) an[r] = (i + r < n) ? L[il(i + r, ln)] : 0.0;
 #pragma unroll
-            for (int r = 0; r < KM; ++r)
-                if (!DIAG || r >= c) acc[r][c] = fma(-a[r], b[c], acc[r][c]);
+            for (int c = 0; c < KN; ++c) bn[c] = (c < nc) ? L[il(k + c, ln)] : 0.0;
+#pragma unroll
+            for (int c = 0; c < KN; ++c)
+#pragma unroll
+                for (int r = 0; r < KM; ++r)
+                    if (!DIAG || r >= c) acc[r][c] = fma(-a[r], b[c], acc[r][c]);
+#pragma unroll
+            for (int r = 0; r < KM; ++r) a[r] = an[r];
+#pragma unroll
+            for (int c = 0; c < KN; ++c) b[c] = bn[c];
+        }
+    } else {
+        for (int l = 0; l < k; ++l) {
+            double a[KM], b[KN];
+#pragma unroll
+            for (int r = 0; r < KM; ++r) a[r] = (i + r < n) ? L[il(i + r, l)] : 0.0;
+#pragma unroll
+            for (int c = 0; c < KN; ++c) b[c] = (c < nc) ? L[il(k + c, l)] : 0.0;
+#pragma unroll
+            for (int c = 0; c < KN; ++c)
+#pragma unroll
+                for (int r = 0; r < KM; ++r)
+                    if (!DIAG || r >= c) acc[r][c] = fma(-a[r], b[c], acc[r][c]);
+        }
     }
 
     if (diag) {
@@ -178,37 +209,44 @@ struct NoStripHook {
 };
 
 // hook.before(k, nc) runs before strip k reads its columns, hook.after(k, nc) once columns
-// k .. k+nc-1 of L are final.
-template <int KN, int TS, class Src, class Addr, class Hook = NoStripHook>
-__device__ int potrf_thread_src(int n, Src const& A, double* L, Addr il, Hook const& hook = Hook{}) {
+// k .. k+nc-1 of L are final. The matrix is m x n with m >= n (BLAST's potrf accepts such
+// trapezoids, dense/Potrf.hpp:78-105: the tiles of every strip run down to row m, so the rows
+// below the top n x n block are solved against its factor). PF selects the tiles' load look-ahead.
+template <int KN, int TS, class Src, class Addr, class Hook = NoStripHook, bool PF = false>
+__device__ int potrf_thread_src_mn(int m, int n, Src const& A, double* L, Addr il, Hook const& hook = Hook{}) {
     int info = 0;
     for (int k = 0; k < n; k += KN) {
         int const nc = min(KN, n - k);
         hook.before(k, nc);
         double y[KN];
         int i = k;
-        while (i < n) {
-            int const rem = n - i;
+        while (i < m) {
+            int const rem = m - i;
             // BLAST's tile cover: 3*TS rows while more than 2*TS remain, then 2*TS while more
             // than TS remain, then TS.
             bool const first = i == k;
             if (rem > 2 * TS) {
-                if (first) potrf_tile<3 * TS, KN, true>(n, k, i, nc, A, L, il, y, info);
-                else potrf_tile<3 * TS, KN, false>(n, k, i, nc, A, L, il, y, info);
+                if (first) potrf_tile<3 * TS, KN, true, PF>(m, k, i, nc, A, L, il, y, info);
+                else potrf_tile<3 * TS, KN, false, PF>(m, k, i, nc, A, L, il, y, info);
                 i += 3 * TS;
             } else if (rem > TS) {
-                if (first) potrf_tile<2 * TS, KN, true>(n, k, i, nc, A, L, il, y, info);
-                else potrf_tile<2 * TS, KN, false>(n, k, i, nc, A, L, il, y, info);
+                if (first) potrf_tile<2 * TS, KN, true, PF>(m, k, i, nc, A, L, il, y, info);
+                else potrf_tile<2 * TS, KN, false, PF>(m, k, i, nc, A, L, il, y, info);
                 i += 2 * TS;
             } else {
-                if (first) potrf_tile<TS, KN, true>(n, k, i, nc, A, L, il, y, info);
-                else potrf_tile<TS, KN, false>(n, k, i, nc, A, L, il, y, info);
+                if (first) potrf_tile<TS, KN, true, PF>(m, k, i, nc, A, L, il, y, info);
+                else potrf_tile<TS, KN, false, PF>(m, k, i, nc, A, L, il, y, info);
                 i += TS;
             }
         }
         hook.after(k, nc);
     }
     return info;
+}
+
+template <int KN, int TS, class Src, class Addr, class Hook = NoStripHook>
+__device__ __forceinline__ int potrf_thread_src(int n, Src const& A, double* L, Addr il, Hook const& hook = Hook{}) {
+    return potrf_thread_src_mn<KN, TS>(n, n, A, L, il, hook);
 }
 
 template <int KN, int TS, class Addr>
@@ -325,16 +363,19 @@ struct PosvArgs {
     int32_t* info;
     int64_t batch;
     int mode;  // 0 potrf, 1 potrf + solves, 2 solves only
+    int m = 0; // rows of A and L for potrf (mode 0) of an m x n trapezoid; 0 means m = n
 };
 
-template <int THREADS, int MINB>
+template <int THREADS, int MINB, bool PF = false>
 __global__ void __launch_bounds__(THREADS, MINB) posv_thread_kernel(PosvArgs p) {
     int64_t const b = (int64_t)blockIdx.x * THREADS + threadIdx.x;
     if (b >= p.batch) return;
     double* L = p.L + b * p.sl;
     int info = 0;
     if (p.mode != 2) {
-        info = potrf_thread<4, 4>(p.n, p.A + b * p.sa, ColAddr{p.lda}, L, ColAddr{p.ldl});
+        int const m = p.m > p.n ? p.m : p.n;
+        info = potrf_thread_src_mn<4, 4, LoadSrc<ColAddr>, ColAddr, NoStripHook, PF>(
+            m, p.n, LoadSrc<ColAddr>{p.A + b * p.sa, ColAddr{p.lda}}, L, ColAddr{p.ldl});
         if (p.info) p.info[b] = info;
     }
     if (p.mode != 0 && p.nrhs > 0) {
@@ -469,15 +510,15 @@ __global__ void __launch_bounds__(32, 12) potrf_desc_kernel(const blastgpu_potrf
     int64_t const b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= count) return;
     blastgpu_potrf_desc const d = desc[b];
-    int const n = d.A.rows;
-    bool const ok = d.A.layout == layout && d.L.layout == layout && d.A.cols == n && d.L.rows == n &&
+    int const m = d.A.rows, n = d.A.cols;  // m >= n: BLAST's trapezoidal potrf
+    bool const ok = d.A.layout == layout && d.L.layout == layout && n <= m && d.L.rows == m &&
                     d.L.cols == n && (layout == BLASTGPU_COL_MAJOR || (d.A.ps == ps && d.L.ps == ps));
     if (!ok) {
         if (info) info[b] = -1;
         return;
     }
     Addr const ia{d.A.ld}, il{d.L.ld};
-    int const r = potrf_thread<KN, TS>(n, d.A.data, ia, d.L.data, il);
+    int const r = potrf_thread_src_mn<KN, TS>(m, n, LoadSrc<Addr>{d.A.data, ia}, d.L.data, il);
     if (info) info[b] = r;
 }
 
@@ -504,24 +545,33 @@ __global__ void __launch_bounds__(32, 12) syrk_potrf_thread_kernel(SyrkPotrfArgs
 
 int launch_posv(PosvArgs const& p, cudaStream_t stream) {
     if (p.batch == 0 || p.n == 0) {
-        if (p.info && p.batch > 0) {
+        if (p.info && p.batch > 0 && p.mode != 2) {
             cudaError_t const e = cudaMemsetAsync(p.info, 0, sizeof(int32_t) * p.batch, stream);
             if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
         }
         return BLASTGPU_SUCCESS;
     }
-    // "posv.variant": CTA size and the occupancy the register allocation is bounded for.
+    // Square matrices from "posv.cta_min_n" (default 65) on go to the CTA-per-matrix kernels: one
+    // thread per matrix would need more registers than a thread has, and a batch of them leaves
+    // most of the chip idle.
+    if ((p.m == 0 || p.m == p.n) && p.n >= tune_get("posv.cta_min_n", 65) && p.n <= 512)
+        return launch_posv_cta_strided(p.n, p.nrhs, p.mode == 2 ? nullptr : p.A, p.lda, p.sa, p.L, p.ldl, p.sl,
+                                       p.B, p.ldb, p.sb, p.X, p.ldx, p.sx, p.mode == 2 ? nullptr : p.info,
+                                       p.batch, stream);
+    // "posv.variant": CTA size and the occupancy the register allocation is bounded for (4: as 3,
+    // with one column of load look-ahead in the factorisation's tile updates).
     // Measured on GB300 at n = 48 (50,000 instances): 32 threads x 12 CTAs/SM is fastest
     // (4.29 ms vs 4.56 ms for 64 x 6 and 5.30 ms for 64 x 1); it lets the block scheduler even
     // out the per-SM load one warp at a time.
     int const variant = tune_get_bin("posv.variant", p.n, 3);
-    int const threads = variant == 2 ? 128 : variant == 3 ? 32 : 64;
+    int const threads = variant == 2 ? 128 : (variant == 3 || variant == 4) ? 32 : 64;
     int64_t const blocks = (p.batch + threads - 1) / threads;
     if (blocks > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
     switch (variant) {
         case 0: posv_thread_kernel<64, 1><<<(unsigned)blocks, 64, 0, stream>>>(p); break;
         case 2: posv_thread_kernel<128, 3><<<(unsigned)blocks, 128, 0, stream>>>(p); break;
         case 3: posv_thread_kernel<32, 12><<<(unsigned)blocks, 32, 0, stream>>>(p); break;
+        case 4: posv_thread_kernel<32, 12, true><<<(unsigned)blocks, 32, 0, stream>>>(p); break;
         default: posv_thread_kernel<64, 6><<<(unsigned)blocks, 64, 0, stream>>>(p); break;
     }
     return check_launch();
@@ -543,6 +593,19 @@ int blastgpu_dpotrf_strided(int n, const double* A, int lda, int64_t stride_a, d
     if (ldl < (n > 0 ? n : 1)) return -6;
     if (batch < 0) return -9;
     PosvArgs p{n, 0, A, lda, stride_a, L, ldl, stride_l, nullptr, 1, 0, nullptr, 1, 0, info, batch, 0};
+    return launch_posv(p, as_cuda(stream));
+}
+
+int blastgpu_dpotrf_mn_strided(int m, int n, const double* A, int lda, int64_t stride_a, double* L, int ldl,
+                               int64_t stride_l, int32_t* info, int64_t batch, blastgpu_stream_t stream) {
+    if (m < 0) return -1;
+    if (n < 0 || n > m) return -2;
+    if (m > 0 && n > 0 && !A) return -3;
+    if (lda < (m > 0 ? m : 1)) return -4;
+    if (m > 0 && n > 0 && !L) return -6;
+    if (ldl < (m > 0 ? m : 1)) return -7;
+    if (batch < 0) return -10;
+    PosvArgs p{n, 0, A, lda, stride_a, L, ldl, stride_l, nullptr, 1, 0, nullptr, 1, 0, info, batch, 0, m};
     return launch_posv(p, as_cuda(stream));
 }
 
@@ -668,7 +731,9 @@ int blastgpu_dsyrk_potrf_strided(int n, int k, int trans_a, double alpha, const 
     // 8.85 ms for the pair vs 9.42 ms fused at 50,000 instances, and the pair is further ahead at
     // smaller batches, so the pair is the default; "syrk_potrf.fused_min_batch" selects the fused
     // kernel from that batch size on.
-    if (batch < tune_get("syrk_potrf.fused_min_batch", 0x7fffffff)) {
+    // Sizes that the potrf entry point sends to the CTA kernels always take the pair, so that the
+    // result stays equal to syrkLower followed by potrf bit for bit.
+    if (batch < tune_get("syrk_potrf.fused_min_batch", 0x7fffffff) || n >= tune_get("posv.cta_min_n", 65)) {
         int st = launch_syrk_lower(n, k, trans_a, alpha, A, lda, stride_a, beta, C, ldc, stride_c, D, ldd,
                                    stride_d, batch, s);
         if (st != BLASTGPU_SUCCESS) return st;

@@ -34,6 +34,37 @@ assert POTRF_DTYPE.itemsize == 64
 COPY_DTYPE = np.dtype([("src", MAT_DTYPE), ("dst", MAT_DTYPE)], align=True)
 assert COPY_DTYPE.itemsize == 64
 
+SYRK_DTYPE = np.dtype([("A", MAT_DTYPE), ("C", MAT_DTYPE), ("D", MAT_DTYPE), ("alpha", "<f8"), ("beta", "<f8")],
+                      align=True)
+assert SYRK_DTYPE.itemsize == 112
+
+TRSM_DTYPE = np.dtype([("A", MAT_DTYPE), ("B", MAT_DTYPE), ("X", MAT_DTYPE)], align=True)
+assert TRSM_DTYPE.itemsize == 96
+
+TRMM_DTYPE = np.dtype([("A", MAT_DTYPE), ("B", MAT_DTYPE), ("C", MAT_DTYPE), ("alpha", "<f8")], align=True)
+assert TRMM_DTYPE.itemsize == 104
+
+GER_DTYPE = np.dtype([("x", MAT_DTYPE), ("y", MAT_DTYPE), ("A", MAT_DTYPE), ("B", MAT_DTYPE), ("alpha", "<f8")],
+                     align=True)
+assert GER_DTYPE.itemsize == 136
+
+LASWP_DTYPE = np.dtype([("A", MAT_DTYPE), ("ipiv", "<u8"), ("k0", "<i4"), ("k1", "<i4")], align=True)
+assert LASWP_DTYPE.itemsize == 48
+
+SWAP_DTYPE = np.dtype([("x", MAT_DTYPE), ("y", MAT_DTYPE)], align=True)
+assert SWAP_DTYPE.itemsize == 64
+
+GEMM_BWD_DTYPE = np.dtype([("A", MAT_DTYPE), ("B", MAT_DTYPE), ("Dbar", MAT_DTYPE), ("Abar", MAT_DTYPE),
+                           ("Bbar", MAT_DTYPE), ("Cbar", MAT_DTYPE), ("alpha", "<f8"), ("beta", "<f8")], align=True)
+assert GEMM_BWD_DTYPE.itemsize == 208
+
+TRSM_BWD_DTYPE = np.dtype([("A", MAT_DTYPE), ("X", MAT_DTYPE), ("Xbar", MAT_DTYPE), ("Bbar", MAT_DTYPE),
+                           ("Abar", MAT_DTYPE)], align=True)
+assert TRSM_BWD_DTYPE.itemsize == 160
+
+POTRF_BWD_DTYPE = np.dtype([("L", MAT_DTYPE), ("Lbar", MAT_DTYPE), ("Abar", MAT_DTYPE)], align=True)
+assert POTRF_BWD_DTYPE.itemsize == 96
+
 EMPTY_MAT = (0, 0, 0, 1, 0, 0, 0)
 
 

@@ -11,7 +11,8 @@
  *   - every pointer to matrix data is a DEVICE pointer (the library never copies host data);
  *   - a batch of one instance is the drop-in for one BLAST call; a "strided" entry point takes
  *     a uniform batch (instance b at base + b*stride), a "batched" entry point takes an array of
- *     per-instance descriptors in device memory (ragged batches: every instance its own sizes);
+ *     per-instance descriptors in device memory (ragged batches: every instance its own sizes
+ *     and layouts); every operation has a "batched" form;
  *   - every call is asynchronous on the given stream, allocates nothing and never synchronises;
  *   - the return value is a status (0 = success; a negative value -i means argument i, counted
  *     from 1, is invalid, LAPACK style; see blastgpu_status); numerical failures are reported per
@@ -215,7 +216,10 @@ int blastgpu_dtrmm_strided(int side, int uplo, int unit, int m, int n, double al
 
 /* ---------------------------------------------------------------------------------------------
  * potrf: lower Cholesky factor L of a symmetric positive definite n x n A (only the lower
- * triangle of A is read; the strict upper triangle of L is not written). L may equal A.
+ * triangle of A is read; the strict upper triangle of L is not written). L may equal A. Uniform
+ * batches with n >= 65 (tuning key posv.cta_min_n) run one CTA per matrix in panels of 32 columns
+ * (the ragged kernels' factorisation), below that one thread per matrix with BLAST's tiles; both
+ * are within 10*n*eps of BLAST's algorithm. The same holds for posv and potrs below.
  * Replaces blast::potrf(A, L) dense (dense/Potrf.hpp:66-106) and panel (panel/Potrf.hpp:59-106).
  * info[b] = 0, or j+1 if the j-th pivot was not positive (BLAST does not check and returns NaNs;
  * the factor is computed the same way and carries the same NaNs). info may be NULL.
@@ -224,9 +228,17 @@ int blastgpu_dpotrf_strided(int n, const double* A, int lda, int64_t stride_a,
                             double* L, int ldl, int64_t stride_l, int32_t* info,
                             int64_t batch, blastgpu_stream_t stream);
 
+/* potrf of m x n trapezoids, m >= n: BLAST's potrf(A, L) accepts them (dense/Potrf.hpp:78-105; it
+ * throws only for columns(A) > rows(A)): the top n x n block is factored and the m - n rows below
+ * it are solved against its factor in the same strips and tiles. A and L are m x n column-major
+ * (L may equal A); info as blastgpu_dpotrf_strided. blastgpu_dpotrf_strided is the case m = n. */
+int blastgpu_dpotrf_mn_strided(int m, int n, const double* A, int lda, int64_t stride_a, double* L, int ldl,
+                               int64_t stride_l, int32_t* info, int64_t batch, blastgpu_stream_t stream);
+
 /* Ragged potrf over descriptors, including BLAST's panel storage. Every descriptor's A and L
  * must have the given layout (BLASTGPU_COL_MAJOR, or BLASTGPU_PANEL with panel height ps = 4
- * (AVX2 panels) or 2 (NEON panels)); instances that do not get info = -1. The panel variants run
+ * (AVX2 panels) or 2 (NEON panels)) and A, L must both be m x n with m >= n (trapezoids as
+ * blastgpu_dpotrf_mn_strided); instances that do not get info = -1. The panel variants run
  * BLAST's panel algorithm (panel/Potrf.hpp:59-106): strips of KN = min((RC-4)/3, SS) columns
  * (4 for ps = 4, 2 for ps = 2), row tiles of 3, 2 and 1 panels. */
 typedef struct blastgpu_potrf_desc {
@@ -349,6 +361,74 @@ int blastgpu_dposv_mixed_batched_noalloc(const blastgpu_posv_desc* desc, int64_t
                                          int32_t* iters, double* berr, blastgpu_stream_t stream);
 
 /* ---------------------------------------------------------------------------------------------
+ * Ragged (descriptor) forms of syrkLower, trsm, trmm and the BLAS-2 operations: one device array
+ * of per-instance descriptors, every operand a blastgpu_mat view of any layout (column-major,
+ * row-major = BLAST's trans() view, panel), so one call takes one instance or a batch of
+ * instances of different sizes and layouts. Per element the order of rounded operations is the
+ * strided entry point's (bit-identical results). status[b] (optional) = 0, or -1 if the
+ * instance's shapes do not fit together (nothing is written for it). A vector operand is a
+ * blastgpu_mat with one column (element i at (i, 0)) or one row (element i at (0, i)), so a
+ * column or a row of a matrix is a vector view too (BLAST's column()/row(),
+ * RowColumnVectorPointer.hpp:179-231).
+ * ------------------------------------------------------------------------------------------- */
+typedef struct blastgpu_syrk_desc {
+    blastgpu_mat A;        /* m x k */
+    blastgpu_mat C, D;     /* m x m; lower triangle of C read, of D written; D may equal C */
+    double alpha, beta;
+} blastgpu_syrk_desc;      /* 112 bytes */
+/* Replaces blast::syrkLower(alpha, A, beta, C, D) (dense/Syrk.hpp:15-145). */
+int blastgpu_dsyrk_lower_batched(const blastgpu_syrk_desc* desc, int64_t batch, int32_t* status,
+                                 blastgpu_stream_t stream);
+
+typedef struct blastgpu_trsm_desc {
+    blastgpu_mat A;        /* triangular, m x m (side LEFT) or n x n (side RIGHT), as viewed */
+    blastgpu_mat B, X;     /* m x n; X may equal B */
+} blastgpu_trsm_desc;      /* 96 bytes */
+/* side = LEFT: A*X = B, replaces blast::trsm<UpLo, UNIT>(A, B, X) (dense/Trsm.hpp:17-66);
+ * side = RIGHT: X*A = B (no BLAST counterpart, see blastgpu_dtrsm_right_strided). uplo names the
+ * triangle of A as viewed (the row-major view of a lower factor is upper: BLAST's
+ * trsm<Upper>(trans(L), ..)); unit = 1: unit diagonal, not read. */
+int blastgpu_dtrsm_batched(int side, int uplo, int unit, const blastgpu_trsm_desc* desc, int64_t batch,
+                           int32_t* status, blastgpu_stream_t stream);
+
+typedef struct blastgpu_trmm_desc {
+    blastgpu_mat A;        /* triangular, m x m (LEFT) or n x n (RIGHT) */
+    blastgpu_mat B, C;     /* m x n; C must not overlap A or B */
+    double alpha;
+} blastgpu_trmm_desc;      /* 104 bytes */
+/* C = alpha*A*B (LEFT) or alpha*B*A (RIGHT); replaces blast::trmm (algorithm/Trmm.hpp:260-310), all
+ * (side, uplo, unit) variants as blastgpu_dtrmm_strided. */
+int blastgpu_dtrmm_batched(int side, int uplo, int unit, const blastgpu_trmm_desc* desc, int64_t batch,
+                           int32_t* status, blastgpu_stream_t stream);
+
+typedef struct blastgpu_ger_desc {
+    blastgpu_mat x, y;     /* vectors of length m and n */
+    blastgpu_mat A, B;     /* m x n; B may equal A */
+    double alpha;
+} blastgpu_ger_desc;       /* 136 bytes */
+/* B = A + alpha*x*y^T (blast::ger, dense/Ger.hpp:40-135). */
+int blastgpu_dger_batched(const blastgpu_ger_desc* desc, int64_t batch, int32_t* status, blastgpu_stream_t stream);
+/* result[b] = first index of the largest |x_i| of vector desc[b] (blast::iamax, dense/Iamax.hpp:66-96),
+ * -1 if desc[b] is not a vector. */
+int blastgpu_idamax_batched(const blastgpu_mat* desc, int64_t batch, int32_t* result, blastgpu_stream_t stream);
+
+typedef struct blastgpu_laswp_desc {
+    blastgpu_mat A;
+    const int32_t* ipiv;   /* device pointer; rows k0 .. k1-1 are swapped with ipiv[k] */
+    int32_t k0, k1;
+} blastgpu_laswp_desc;     /* 48 bytes */
+/* blast::laswp (dense/Laswp.hpp:37-43) on every column of A; an instance whose ipiv[k0..k1-1] names
+ * a row outside A gets status -1 and is left unchanged. */
+int blastgpu_dlaswp_batched(const blastgpu_laswp_desc* desc, int64_t batch, int32_t* status,
+                            blastgpu_stream_t stream);
+
+typedef struct blastgpu_swap_desc {
+    blastgpu_mat x, y;     /* vectors of the same length */
+} blastgpu_swap_desc;      /* 64 bytes */
+/* blast::swap (dense/Swap.hpp:35-44). */
+int blastgpu_dswap_batched(const blastgpu_swap_desc* desc, int64_t batch, int32_t* status, blastgpu_stream_t stream);
+
+/* ---------------------------------------------------------------------------------------------
  * Adjoints (no BLAST counterpart). For X = A^{-1} B with A SPD and a scalar loss l:
  *   dl/dB = A^{-1} dl/dX,   dl/dA = -(dl/dB X^T + X dl/dB^T) / 2  (symmetrised),
  * from the forward factor L (recompute = 0), or recomputing L from A into the L matrix
@@ -396,6 +476,35 @@ int blastgpu_dtrsm_bwd_strided(int uplo, int trans_a, int unit, int m, int n, co
  * blastgpu_dposv_bwd_batched. Abar must not alias L or Lbar; for batch > 1 its stride is not 0. */
 int blastgpu_dpotrf_bwd_strided(int n, const double* L, int ldl, int64_t stride_l, const double* Lbar, int ldlb,
                                 int64_t stride_lb, double* Abar, int ldab, int64_t stride_ab, int64_t batch,
+                                blastgpu_stream_t stream);
+
+/* Ragged forms of the three adjoints (no BLAST counterpart). Operands are views (A, B as the
+ * forward call saw them, so op() is the view), gradients are views in their operand's own
+ * orientation; a gradient with data = NULL is not wanted. status as the ragged forms above
+ * (-1 also for a transposed product over panel storage, which has no transposed view).
+ *   gemm:  Abar += alpha*Dbar*B^T, Bbar += alpha*A^T*Dbar, Cbar += beta*Dbar  (accumulate);
+ *          max_dim bounds every instance's m, n and k (it selects the gemm tiling);
+ *   trsm:  A*X = B (left, uplo/unit of A as viewed): Bbar = A^{-T}*Xbar (written; may equal Xbar),
+ *          Abar -= Bbar*X^T on A's triangle (accumulated; optional);
+ *   potrf: Abar = (S + S^T)/2, S = L^{-T} Phi(L^T*Lbar) L^{-1} (written in full). */
+typedef struct blastgpu_gemm_bwd_desc {
+    blastgpu_mat A, B, Dbar;         /* m x k, k x n, m x n */
+    blastgpu_mat Abar, Bbar, Cbar;   /* m x k, k x n, m x n (each optional) */
+    double alpha, beta;
+} blastgpu_gemm_bwd_desc;            /* 208 bytes */
+int blastgpu_dgemm_bwd_batched(const blastgpu_gemm_bwd_desc* desc, int64_t batch, int max_dim, int32_t* status,
+                               blastgpu_stream_t stream);
+
+typedef struct blastgpu_trsm_bwd_desc {
+    blastgpu_mat A, X, Xbar, Bbar, Abar;   /* m x m, m x n, m x n, m x n, m x m (Abar optional) */
+} blastgpu_trsm_bwd_desc;                  /* 160 bytes */
+int blastgpu_dtrsm_bwd_batched(int uplo, int unit, const blastgpu_trsm_bwd_desc* desc, int64_t batch,
+                               int32_t* status, blastgpu_stream_t stream);
+
+typedef struct blastgpu_potrf_bwd_desc {
+    blastgpu_mat L, Lbar, Abar;            /* n x n each; Abar must not alias L or Lbar */
+} blastgpu_potrf_bwd_desc;                 /* 96 bytes */
+int blastgpu_dpotrf_bwd_batched(const blastgpu_potrf_bwd_desc* desc, int64_t batch, int32_t* status,
                                 blastgpu_stream_t stream);
 
 #ifdef __cplusplus

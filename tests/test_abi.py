@@ -175,6 +175,15 @@ def test_descriptor_layouts_match_header(tmp_path):
         "blastgpu_posv_bwd_desc": (desc.POSV_BWD_DTYPE, ["A", "L", "X", "Xbar", "Bbar", "Abar"]),
         "blastgpu_potrf_desc": (desc.POTRF_DTYPE, ["A", "L"]),
         "blastgpu_copy_desc": (desc.COPY_DTYPE, ["src", "dst"]),
+        "blastgpu_syrk_desc": (desc.SYRK_DTYPE, ["A", "C", "D", "alpha", "beta"]),
+        "blastgpu_trsm_desc": (desc.TRSM_DTYPE, ["A", "B", "X"]),
+        "blastgpu_trmm_desc": (desc.TRMM_DTYPE, ["A", "B", "C", "alpha"]),
+        "blastgpu_ger_desc": (desc.GER_DTYPE, ["x", "y", "A", "B", "alpha"]),
+        "blastgpu_laswp_desc": (desc.LASWP_DTYPE, ["A", "ipiv", "k0", "k1"]),
+        "blastgpu_swap_desc": (desc.SWAP_DTYPE, ["x", "y"]),
+        "blastgpu_gemm_bwd_desc": (desc.GEMM_BWD_DTYPE, ["A", "B", "Dbar", "Abar", "Bbar", "Cbar", "alpha", "beta"]),
+        "blastgpu_trsm_bwd_desc": (desc.TRSM_BWD_DTYPE, ["A", "X", "Xbar", "Bbar", "Abar"]),
+        "blastgpu_potrf_bwd_desc": (desc.POTRF_BWD_DTYPE, ["L", "Lbar", "Abar"]),
     }
     lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "blastgpu.h"', "int main(void) {"]
     for name, (_, fields) in structs.items():

@@ -217,3 +217,40 @@ def test_getrs_large_n_bitexact(gpu, oracle_lib, n):
         Xr = np.asfortranarray(B[b].copy())
         oracle_lib.getrs(LUr, pr, Xr, Xr)
         assert np.array_equal(X[b], Xr), n
+
+
+def test_getrf_kernel_choice_keeps_bits(gpu, oracle_lib):
+    """The autotuner's per-bin choice between the warp-per-matrix and CTA-per-matrix LU kernels
+    ("getrf.cta.n<bin>") changes the schedule, never the result: factors and pivots are identical
+    under both choices and equal to the oracle's."""
+    import torch
+
+    from blast_gb300 import _lib
+    from blast_gb300.ragged import GesvPlan, Packed
+
+    rng = np.random.default_rng(91)
+    ns = [7, 40, 65, 100, 129, 200, 256, 31]
+    mats = [rng.standard_normal((n, n)) for n in ns]
+    results = []
+    for choice in (0, 1):
+        for b in (8, 16, 32, 64, 128, 256):
+            _lib.tune_set(f"getrf.cta.n{b}", choice)
+        try:
+            A = Packed(ns, ns, "cuda")
+            A.fill_from(mats)
+            B = Packed(ns, [1] * len(ns), "cuda")
+            B.fill_from([np.ones((n, 1)) for n in ns])
+            plan = GesvPlan(A, B)
+            plan.run()
+            torch.cuda.synchronize()
+            results.append((A.to_list(), plan.pivots(), B.to_list()))
+        finally:
+            for b in (8, 16, 32, 64, 128, 256):
+                _lib.tune_set(f"getrf.cta.n{b}", 1 if b > 64 else 0)
+    (LU0, P0, X0), (LU1, P1, X1) = results
+    for i, n in enumerate(ns):
+        assert np.array_equal(LU0[i], LU1[i]) and np.array_equal(P0[i], P1[i]) and np.array_equal(X0[i], X1[i])
+        LUr = np.asfortranarray(mats[i].copy())
+        pr = np.zeros(n, dtype=np.int32)
+        oracle_lib.getrf(LUr, pr)
+        assert np.array_equal(LU0[i], LUr) and np.array_equal(P0[i], pr)
