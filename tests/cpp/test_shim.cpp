@@ -122,6 +122,141 @@ int main() {
         CHECK(idx == want);
     }
 
+    // BLAST's matrix types on the device: StaticMatrix / DynamicMatrix (column-major) and
+    // StaticPanelMatrix / DynamicPanelMatrix (panels of 4 rows), all through the descriptor calls
+    {
+        blastgpu::DescriptorArena arena;
+        int const m = 13;
+        std::vector<double> G(m * m), Sm(m * m);
+        for (auto& v : G) v = U(gen);
+        for (int i = 0; i < m; ++i)
+            for (int j = 0; j < m; ++j) {
+                double s = i == j ? m : 0.0;
+                for (int k = 0; k < m; ++k) s += G[i + k * m] * G[j + k * m];
+                Sm[i + j * m] = s;
+            }
+        blastgpu::StaticMatrix<13, 13> sA;
+        blastgpu::DynamicMatrix dL(m, m);
+        blastgpu::StaticPanelMatrix<13, 13, 4> pA;
+        blastgpu::DynamicPanelMatrix pL(m, m, 4);
+        CHECK(sA.rows() == 13 && pA.spacing() == 52 && pL.spacing() == 52 && dL.spacing() == 13);
+        blastgpu::copy_to_device(sA, Sm.data());
+        blastgpu::copy_to_device(pA, Sm.data());
+        // dense and panel potrf give the same factor to rounding (both follow BLAST's algorithm)
+        blastgpu::potrf(blastgpu::Matrix(sA), blastgpu::Matrix(dL), nullptr, arena);
+        blastgpu::potrf(blastgpu::Matrix(pA), blastgpu::Matrix(pL), nullptr, arena);
+        CHECK(cudaDeviceSynchronize() == cudaSuccess);
+        std::vector<double> L1(m * m), L2(m * m);
+        blastgpu::copy_to_host(dL, L1.data());
+        blastgpu::copy_to_host(pL, L2.data());
+        for (int j = 0; j < m; ++j)
+            for (int i = j; i < m; ++i) {
+                double r = Sm[i + j * m];
+                for (int k = 0; k <= j; ++k) r -= L1[i + k * m] * L1[j + k * m];
+                CHECK(std::fabs(r) < 1e-11 * m);
+                CHECK(std::fabs(L1[i + j * m] - L2[i + j * m]) < 1e-13 * m);
+            }
+        // panel gemm: D = L * trans(L) with L in panel storage, trans(L) the row-major view of dL
+        // (whose upper triangle is zero from its zero-filled construction)
+        blastgpu::DynamicMatrix dD(m, m), dZ(m, m);
+        blastgpu::DynamicPanelMatrix pLt(m, m, 4);
+        std::vector<double> Lsym(m * m, 0.0);
+        for (int j = 0; j < m; ++j)
+            for (int i = j; i < m; ++i) Lsym[i + j * m] = L2[i + j * m];
+        blastgpu::copy_to_device(pLt, Lsym.data());
+        blastgpu::gemm(1.0, blastgpu::Matrix(pLt), blastgpu::trans(blastgpu::Matrix(dL)), 0.0, blastgpu::Matrix(dZ),
+                       blastgpu::Matrix(dD), arena);
+        CHECK(cudaDeviceSynchronize() == cudaSuccess);
+        std::vector<double> Dh(m * m);
+        blastgpu::copy_to_host(dD, Dh.data());
+        for (int i = 0; i < m * m; ++i) CHECK(std::fabs(Dh[i] - Sm[i]) < 1e-11 * m);
+
+        // row() and column() views: swap row 2 of a panel matrix with column 5 of a dense one
+        blastgpu::DynamicMatrix dV(m, m);
+        std::vector<double> V(m * m), P(m * m);
+        for (auto& v : V) v = U(gen);
+        for (auto& v : P) v = U(gen);
+        blastgpu::DynamicPanelMatrix pP(m, m, 4);
+        blastgpu::copy_to_device(dV, V.data());
+        blastgpu::copy_to_device(pP, P.data());
+        blastgpu::Matrix const r2 = blastgpu::row(blastgpu::Matrix(pP), 2), c5 = blastgpu::column(blastgpu::Matrix(dV), 5);
+        CHECK(r2.rows == 1 && r2.cols == m && c5.rows == m && c5.cols == 1);
+        std::vector<blastgpu_swap_desc> sds{blastgpu_swap_desc{blastgpu::to_mat(r2), blastgpu::to_mat(c5)}};
+        CHECK(blastgpu_dswap_batched(arena.upload(sds, nullptr), 1, nullptr, nullptr) == BLASTGPU_SUCCESS);
+        CHECK(cudaDeviceSynchronize() == cudaSuccess);
+        std::vector<double> V2(m * m), P2(m * m);
+        blastgpu::copy_to_host(dV, V2.data());
+        blastgpu::copy_to_host(pP, P2.data());
+        for (int j = 0; j < m; ++j) CHECK(P2[2 + j * m] == V[j + 5 * m] && V2[j + 5 * m] == P[2 + j * m]);
+        blastgpu::Vector const rv = blastgpu::as_vector(blastgpu::row(blastgpu::Matrix(dV), 1));
+        CHECK(rv.size == m && rv.inc == m);
+
+        // a ragged batch of different sizes: gemm, potrf, trsm<Lower>/<Upper>, syrkLower per instance
+        std::vector<blastgpu::DynamicMatrix> store;
+        std::vector<blastgpu::Matrix> RA, RB, RC, RD, RS, RL, RX;
+        int const sizes[3] = {3, 17, 40};
+        std::vector<std::vector<double>> hA(3), hB(3), hS(3);
+        for (int t = 0; t < 3; ++t) {
+            int const q = sizes[t];
+            hA[t].resize(q * q);
+            hB[t].resize(q * 2);
+            for (auto& v : hA[t]) v = U(gen);
+            for (auto& v : hB[t]) v = U(gen);
+            hS[t].assign(q * q, 0.0);
+            for (int i = 0; i < q; ++i)
+                for (int j = 0; j < q; ++j) {
+                    double s = i == j ? q : 0.0;
+                    for (int k = 0; k < q; ++k) s += hA[t][i + k * q] * hA[t][j + k * q];
+                    hS[t][i + j * q] = s;
+                }
+        }
+        store.reserve(18);
+        for (int t = 0; t < 3; ++t)
+            for (int w = 0; w < 6; ++w) store.emplace_back(sizes[t], w == 1 || w == 5 ? 2 : sizes[t]);
+        for (int t = 0; t < 3; ++t) {
+            blastgpu::Matrix a = store[6 * t], d = store[6 * t + 2], s2 = store[6 * t + 3], l = store[6 * t + 4],
+                             x = store[6 * t + 5];
+            blastgpu::copy_to_device(a, hA[t].data());
+            blastgpu::copy_to_device(s2, hS[t].data());
+            blastgpu::copy_to_device(x, hB[t].data());
+            RA.push_back(a);
+            RB.push_back(blastgpu::trans(a));
+            RC.push_back(s2);
+            RD.push_back(d);
+            RS.push_back(s2);
+            RL.push_back(l);
+            RX.push_back(x);
+        }
+        blastgpu::gemm(1.0, RA, RB, 0.0, RC, RD, arena);        // D = A * A^T
+        blastgpu::potrf(RS, RL, nullptr, arena);                // L = chol(S)
+        blastgpu::trsm<blastgpu::UpLo::Lower, false>(RL, RX, RX, arena);
+        std::vector<blastgpu::Matrix> RLt;
+        for (auto const& l : RL) RLt.push_back(blastgpu::trans(l));
+        blastgpu::trsm<blastgpu::UpLo::Upper, false>(RLt, RX, RX, arena);  // X = S^{-1} B
+        blastgpu::syrkLower(1.0, RA, 1.0, RD, RD, arena);      // D_lower += A A^T
+        CHECK(cudaDeviceSynchronize() == cudaSuccess);
+        for (int t = 0; t < 3; ++t) {
+            int const q = sizes[t];
+            std::vector<double> Dg(q * q), Xg(q * 2);
+            blastgpu::copy_to_host(RD[t], Dg.data());
+            blastgpu::copy_to_host(RX[t], Xg.data());
+            for (int j = 0; j < q; ++j)
+                for (int i = 0; i < q; ++i) {
+                    double const aat = hS[t][i + j * q] - (i == j ? q : 0.0);
+                    CHECK(std::fabs(Dg[i + j * q] - (i >= j ? 2.0 : 1.0) * aat) < 1e-12 * q);
+                }
+            for (int c = 0; c < 2; ++c)
+                for (int i = 0; i < q; ++i) {
+                    double r = hB[t][i + c * q];
+                    for (int j = 0; j < q; ++j) r -= hS[t][i + j * q] * Xg[j + c * q];
+                    CHECK(std::fabs(r) < 1e-11 * q);
+                }
+        }
+        bool threw2 = false;
+        try { blastgpu::trans(blastgpu::Matrix(pA)); } catch (std::logic_error const&) { threw2 = true; }
+        CHECK(threw2);
+    }
+
     // size mismatch and unimplemented variants throw BLAST's exception types
     threw = false;
     try { blastgpu::gemm(bt(dA), blastgpu::batch(blastgpu::matrix(dB, n - 1, n)), bt(dC), bt(dD)); }
