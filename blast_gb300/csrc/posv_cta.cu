@@ -305,6 +305,64 @@ __device__ __forceinline__ void cta_chol_block(T* blk, int nb, int k0, T* rinv, 
     }
 }
 
+// The second half of one panel step, shared by every factorisation below: the panel (rows
+// k0 .. n-1, nb columns) is in shared memory at buf (column c at buf + c * NMAX), already updated
+// with all previous columns. Factors its nb x nb diagonal block, solves the rows below against
+// it, and writes the panel to F. With blk64 (binary32 factor only), the diagonal block is factored
+// in binary64: widened into blk64 (32 x 32 doubles), factored column at a time, and rounded back.
+template <typename T, int NMAX>
+__device__ __forceinline__ void cta_panel_finish(T* buf, int nb, int m, int k0, T* F, int ldf, T* rinv,
+                                                 int* s_info, double* blk64 = nullptr) {
+    int const tid = threadIdx.x;
+    if (blk64 != nullptr) {
+        double* rinv64 = blk64 + 32 * 32;
+        for (int e = tid; e < 32 * 32; e += kThreads) {
+            int const c = e >> 5, r = e & 31;
+            blk64[e] = (r < nb && c < nb && r >= c) ? (double)buf[c * NMAX + r] : 0.0;
+        }
+        __syncthreads();
+        cta_chol_block_cols<double, 32>(blk64, nb, k0, rinv64, s_info);
+        for (int e = tid; e < 32 * 32; e += kThreads) {
+            int const c = e >> 5, r = e & 31;
+            if (r < nb && c < nb && r >= c) buf[c * NMAX + r] = (T)blk64[e];
+        }
+        if (tid < nb) rinv[tid] = (T)rinv64[tid];
+        __syncthreads();
+    } else {
+        // Diagonal block (nb x nb), all threads, in shared memory.
+        cta_chol_block<T, NMAX>(buf, nb, k0, rinv, s_info);
+    }
+    // Rows below the block: x_j = (p_j - sum_{q<j} x_q l_jq) / l_jj, one thread per row, the
+    // row in registers and the block's entries broadcast from shared memory.
+    for (int r = nb + tid; r < m; r += kThreads) {
+        T x[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            if (j < nb) {
+                T v = buf[j * NMAX + r];
+#pragma unroll
+                for (int q = 0; q < j; ++q) v = fma(-x[q], buf[q * NMAX + j], v);
+                x[j] = v * rinv[j];
+                buf[j * NMAX + r] = x[j];
+            }
+        }
+    }
+    __syncthreads();
+    // Panel to the factor (lower part), four columns per pass with their shared-memory loads
+    // issued before the stores.
+    for (int cb = 0; cb < nb; cb += 4) {
+        for (int r = cb + tid; r < m; r += kThreads) {
+            T v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) v[u] = (cb + u < nb && r >= cb + u) ? buf[(cb + u) * NMAX + r] : (T)0;
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (cb + u < nb && r >= cb + u) F[(k0 + r) + (int64_t)(k0 + cb + u) * ldf] = v[u];
+        }
+    }
+    __syncthreads();
+}
+
 // Left-looking blocked Cholesky of the n x n matrix: lower(A) -> F (precision T, ld ldf).
 // Returns info (0 or first bad pivot + 1) identically in all threads. With rowsum (n doubles in
 // shared memory, zeroed by the caller), also accumulates the row sums of |A| of the symmetric
@@ -313,7 +371,7 @@ __device__ __forceinline__ void cta_chol_block(T* blk, int nb, int k0, T* rinv, 
 // the staging buffer, and one thread per row adds them up.
 template <typename T, int MAXR>
 __device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf, int* s_info,
-                         double* rowsum = nullptr) {
+                         double* rowsum = nullptr, double* blk64 = nullptr) {
     constexpr int NMAX = 32 * MAXR;
     __shared__ T rinv[kNB];
     int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -385,37 +443,7 @@ __device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf,
             }
         }
         __syncthreads();
-        // Diagonal block (nb x nb), all threads, in shared memory.
-        cta_chol_block<T, NMAX>(buf, nb, k0, rinv, s_info);
-        // Rows below the block: x_j = (p_j - sum_{q<j} x_q l_jq) / l_jj, one thread per row, the
-        // row in registers and the block's entries broadcast from shared memory.
-        for (int r = nb + tid; r < m; r += kThreads) {
-            T x[32];
-#pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                if (j < nb) {
-                    T v = buf[j * NMAX + r];
-#pragma unroll
-                    for (int q = 0; q < j; ++q) v = fma(-x[q], buf[q * NMAX + j], v);
-                    x[j] = v * rinv[j];
-                    buf[j * NMAX + r] = x[j];
-                }
-            }
-        }
-        __syncthreads();
-        // Panel to the factor (lower part), four columns per pass with their shared-memory loads
-        // issued before the stores.
-        for (int cb = 0; cb < nb; cb += 4) {
-            for (int r = cb + tid; r < m; r += kThreads) {
-                T v[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) v[u] = (cb + u < nb && r >= cb + u) ? buf[(cb + u) * NMAX + r] : (T)0;
-#pragma unroll
-                for (int u = 0; u < 4; ++u)
-                    if (cb + u < nb && r >= cb + u) F[(k0 + r) + (int64_t)(k0 + cb + u) * ldf] = v[u];
-            }
-        }
-        __syncthreads();
+        cta_panel_finish<T, NMAX>(buf, nb, m, k0, F, ldf, rinv, s_info, blk64);
     }
     return *s_info;
 }
