@@ -245,33 +245,12 @@ __device__ int cta_getrf(GetrfItem it, int* s_ret, double* sp) {
             }
         }
         __syncthreads();
-        // A22 := A22 - A21 * U12, thread per row, JB columns at a time: the U12 entries (rows
-        // k..k+3, the same for every thread) and the JB elements of the row are all loaded before
-        // any is updated, so that the loads of a group overlap instead of each read-modify-write
-        // waiting for the last. Rows of U12 and of A22 never overlap, so the order is safe.
-        constexpr int JB = 8;
+        // A22 := A22 - A21 * U12, thread per row
         for (int i = k + NB + tid; i < M; i += kCtaThreads) {
             double l[NB];
 #pragma unroll
             for (int q = 0; q < NB; ++q) l[q] = a[i + (int64_t)(k + q) * lda];
-            int j = k + NB;
-            for (; j + JB <= N; j += JB) {
-                double u[JB][NB], c[JB];
-#pragma unroll
-                for (int jj = 0; jj < JB; ++jj) {
-#pragma unroll
-                    for (int q = 0; q < NB; ++q) u[jj][q] = a[(k + q) + (int64_t)(j + jj) * lda];
-                    c[jj] = a[i + (int64_t)(j + jj) * lda];
-                }
-#pragma unroll
-                for (int jj = 0; jj < JB; ++jj) {
-                    double acc = 0.0;
-#pragma unroll
-                    for (int q = 0; q < NB; ++q) acc = fma(l[q], u[jj][q], acc);
-                    a[i + (int64_t)(j + jj) * lda] = fma(1.0, c[jj], -acc);
-                }
-            }
-            for (; j < N; ++j) {
+            for (int j = k + NB; j < N; ++j) {
                 double const* u = a + k + (int64_t)j * lda;
                 double acc = 0.0;
 #pragma unroll
