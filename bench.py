@@ -926,9 +926,10 @@ def main():
     ap.add_argument("--only-mixed", action="store_true",
                     help="run only the FP64-vs-mixed comparison (with --mixed-count matrices)")
     ap.add_argument("--mixed-count", type=int, default=8192)
-    ap.add_argument("--mixed-mode", type=int, choices=[0, 1, 2], default=None,
+    ap.add_argument("--mixed-mode", type=int, choices=[0, 1, 2, 3], default=None,
                     help="mixed factorisation for --only-mixed: 0 binary32 CUDA cores, 1 tensor cores "
-                         "(3xTF32), 2 tensor cores with binary64 diagonal blocks (default: the library's)")
+                         "(3xTF32), 2 tensor cores with binary64 diagonal blocks, 3 CUDA cores with "
+                         "binary64 diagonal blocks (default: the library's)")
     ap.add_argument("--mixed-gen", choices=["qr", "gram"], default="qr",
                     help="qr: the workload's Q diag(lambda) Q^T matrices; gram: G G^T/n + I, for "
                          "profilers under which torch.linalg cannot load")

@@ -32,6 +32,7 @@
 
 #include <atomic>
 #include <mutex>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -448,6 +449,247 @@ __device__ int cta_potrf(int n, const double* A, int lda, T* F, int ldf, T* buf,
     return *s_info;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Tensor-core panel update for the binary32 factor (mixed path, modes 1 and 2).
+//
+// The update of panel k0 is the rank-k0 product P = F(k0:n, 0:k0) * F(k0:k0+32, 0:k0)^T
+// subtracted from the panel of A: a (n-k0) x 32 x k0 gemm. It runs on the tensor cores as
+// mma.sync m16n8k8 with TF32 operands and binary32 accumulation, in the 3xTF32 scheme: every
+// binary32 operand x is split into x_hi = tf32(x) and x_lo = tf32(x - x_hi) (exact in binary32),
+// and a*b is formed as a_lo*b_hi + a_hi*b_lo + a_hi*b_hi (the a_lo*b_lo term, about 2^-22 of
+// a*b, is dropped); plain TF32 (about 2^-11) would stop the refinement from converging at
+// cond(A) = 1e6. The accumulators start from the panel of A and take -F(i, k) (negation is
+// exact), so D = A - P directly.
+//
+// Accumulator layout (mma's C fragment): warp w owns the row tiles rt = (w >> 1) + 4s (16 rows
+// each) and the column tiles 2(w & 1) and 2(w & 1) + 1 (8 columns each) of the 32-column panel;
+// lane (g = lane >> 2, t = lane & 3) holds rows 16rt + g (+8) and columns 2t, 2t + 1 of a tile.
+// The previous columns are staged through shared memory with cp.async as in panel_update, 16 at
+// a time and double-buffered, with a padded column stride (NMAX + 8 floats) so that the
+// fragment reads are free of bank conflicts.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ void tf32_split(float x, uint32_t& hi, uint32_t& lo) {
+    uint32_t h, l;
+    asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(h) : "f"(x));
+    float const rest = x - __uint_as_float(h);
+    asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(l) : "f"(rest));
+    hi = h;
+    lo = l;
+}
+
+__device__ __forceinline__ void mma_tf32(float (&d)[4], uint32_t const (&a)[4], uint32_t b0, uint32_t b1) {
+    asm("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+        "{%0, %1, %2, %3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+template <int MAXR>
+struct TcShape {
+    static constexpr int NMAX = 32 * MAXR;
+    static constexpr int SP = NMAX + 8;                     // padded column stride of the staging buffer
+    static constexpr int RT = MAXR >= 2 ? MAXR / 2 : 1;     // row tiles per warp (rows <= NMAX)
+    static constexpr int kStageElems = kKC * SP;
+};
+
+template <int MAXR>
+__device__ __forceinline__ void tc_stage(const float* F, int ldf, float* buf, int k0, int m, int ch) {
+    constexpr int SP = TcShape<MAXR>::SP, KH = kKC / 2;
+    int const kk = ch * KH;
+    float* dst = buf + (ch & 1) * KH * SP;
+    for (int q = 0; q < KH; ++q) {
+        float const* src = F + k0 + (int64_t)(kk + q) * ldf;
+        for (int r = threadIdx.x; r < m; r += kThreads) cp_async(dst + q * SP + r, src + r);
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+// R = row tiles this panel needs per warp (ceil(ceil(m / 16) / 4)), fixed at compile time.
+template <int R, int MAXR>
+__device__ __forceinline__ void tc_panel_update(float (&acc)[TcShape<MAXR>::RT][2][4], const float* F, int ldf,
+                                                float* buf, int k0, int m) {
+    constexpr int SP = TcShape<MAXR>::SP, KH = kKC / 2;
+    int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int const g = lane >> 2, t = lane & 3, rg = warp >> 1, cp = warp & 1;
+    int const rows16 = (m + 15) >> 4;
+    int const nch = k0 / KH;  // k0 is a multiple of the panel width, so every chunk is full
+    if (nch == 0) return;
+    __syncthreads();  // the buffer's earlier contents are no longer read
+    tc_stage<MAXR>(F, ldf, buf, k0, m, 0);
+    for (int ch = 0; ch < nch; ++ch) {
+        if (ch + 1 < nch) {
+            tc_stage<MAXR>(F, ldf, buf, k0, m, ch + 1);
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        }
+        __syncthreads();
+        float const* base = buf + (ch & 1) * KH * SP;
+#pragma unroll
+        for (int ks = 0; ks < KH / 8; ++ks) {
+            float const* col = base + (8 * ks + t) * SP;  // column 8ks + t; column 8ks + t + 4 at col + 4 SP
+            uint32_t bh[2][2], bl[2][2];
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                int const cb = 16 * cp + 8 * j + g;
+                tf32_split(col[cb], bh[j][0], bl[j][0]);
+                tf32_split(col[4 * SP + cb], bh[j][1], bl[j][1]);
+            }
+            // Row tiles in pairs: the three products of the pair's four tiles are issued term by
+            // term, so that the instructions updating one accumulator are four apart and the
+            // ones in between are independent.
+            int const live = min(R, (rows16 - rg + 3) >> 2);  // this warp's row tiles below the diagonal
+#pragma unroll
+            for (int s0 = 0; s0 < R; s0 += 2) {
+                if (s0 < live) {  // warp-uniform
+                    uint32_t ah[2][4], al[2][4];
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+                        int const r0 = 16 * (rg + 4 * (s0 + u)) + g;
+                        tf32_split(-col[r0], ah[u][0], al[u][0]);
+                        tf32_split(-col[r0 + 8], ah[u][1], al[u][1]);
+                        tf32_split(-col[4 * SP + r0], ah[u][2], al[u][2]);
+                        tf32_split(-col[4 * SP + r0 + 8], ah[u][3], al[u][3]);
+                    }
+                    bool const two = s0 + 1 < live && s0 + 1 < R;
+#pragma unroll
+                    for (int u = 0; u < 2; ++u)
+                        if (u == 0 || two)
+#pragma unroll
+                            for (int j = 0; j < 2; ++j)
+                                mma_tf32(acc[s0 + u < R ? s0 + u : s0][j], al[u], bh[j][0], bh[j][1]);
+#pragma unroll
+                    for (int u = 0; u < 2; ++u)
+                        if (u == 0 || two)
+#pragma unroll
+                            for (int j = 0; j < 2; ++j)
+                                mma_tf32(acc[s0 + u < R ? s0 + u : s0][j], ah[u], bl[j][0], bl[j][1]);
+#pragma unroll
+                    for (int u = 0; u < 2; ++u)
+                        if (u == 0 || two)
+#pragma unroll
+                            for (int j = 0; j < 2; ++j)
+                                mma_tf32(acc[s0 + u < R ? s0 + u : s0][j], ah[u], bh[j][0], bh[j][1]);
+                }
+            }
+        }
+        __syncthreads();  // every thread is done with this half before chunk ch + 2 is staged into it
+    }
+}
+
+template <int MAXR>
+__device__ __forceinline__ void tc_panel_update_dispatch(float (&acc)[TcShape<MAXR>::RT][2][4], const float* F,
+                                                         int ldf, float* buf, int k0, int m) {
+    int const rows16 = (m + 15) >> 4;
+    switch ((rows16 + 3) >> 2) {
+#define BLASTGPU_TC_CASE(R) \
+    case R:                 \
+        if constexpr (R <= TcShape<MAXR>::RT) tc_panel_update<R, MAXR>(acc, F, ldf, buf, k0, m); \
+        break;
+        BLASTGPU_TC_CASE(1) BLASTGPU_TC_CASE(2) BLASTGPU_TC_CASE(3) BLASTGPU_TC_CASE(4)
+        BLASTGPU_TC_CASE(5) BLASTGPU_TC_CASE(6) BLASTGPU_TC_CASE(7) BLASTGPU_TC_CASE(8)
+#undef BLASTGPU_TC_CASE
+        default: break;
+    }
+}
+
+// Binary32 left-looking Cholesky with the tensor-core panel update: lower(A) -> F, the same panel
+// steps as cta_potrf<float> (and the same row sums of |A| when rowsum is given).
+template <int MAXR>
+__device__ int cta_potrf_tc(int n, const double* A, int lda, float* F, int ldf, float* buf, int* s_info,
+                            double* rowsum, double* blk64) {
+    constexpr int NMAX = 32 * MAXR, RT = TcShape<MAXR>::RT;
+    __shared__ float rinv[kNB];
+    int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    int const g = lane >> 2, t = lane & 3, rg = warp >> 1, cp = warp & 1;
+    if (tid == 0) *s_info = 0;
+    for (int k0 = 0; k0 < n; k0 += kNB) {
+        int const nb = min(kNB, n - k0);
+        int const m = n - k0;
+        float acc[RT][2][4];
+        // The panel of A (lower part) into the accumulators, all loads issued before any use.
+#pragma unroll
+        for (int s = 0; s < RT; ++s)
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    int const r = 16 * (rg + 4 * s) + g + 8 * (e >> 1);
+                    int const c = 16 * cp + 8 * j + 2 * t + (e & 1);
+                    acc[s][j][e] =
+                        (r < m && c < nb && r >= c) ? (float)A[(k0 + r) + (int64_t)(k0 + c) * lda] : 0.f;
+                }
+        if (rowsum) {
+            // part[cp][r]: row sums over this column pair's 16 columns; colp[rg][c]: column sums
+            // strictly below the diagonal over this row group's rows.
+            double* part = reinterpret_cast<double*>(buf);
+            double* colp = part + 2 * NMAX;
+#pragma unroll
+            for (int s = 0; s < RT; ++s)
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    float rs = fabsf(acc[s][0][2 * h]) + fabsf(acc[s][0][2 * h + 1]) + fabsf(acc[s][1][2 * h]) +
+                               fabsf(acc[s][1][2 * h + 1]);
+                    rs += __shfl_xor_sync(0xffffffffu, rs, 1);
+                    rs += __shfl_xor_sync(0xffffffffu, rs, 2);
+                    int const r = 16 * (rg + 4 * s) + g + 8 * h;
+                    if (t == 0 && r < m) part[cp * NMAX + r] = rs;
+                }
+            float cs[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll
+            for (int s = 0; s < RT; ++s)
+#pragma unroll
+                for (int j = 0; j < 2; ++j)
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        int const r = 16 * (rg + 4 * s) + g + 8 * (e >> 1);
+                        int const c = 16 * cp + 8 * j + 2 * t + (e & 1);
+                        if (r > c) cs[j][e & 1] += fabsf(acc[s][j][e]);
+                    }
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
+#pragma unroll
+                for (int b = 0; b < 2; ++b) {
+                    float v = cs[j][b];
+                    v += __shfl_xor_sync(0xffffffffu, v, 4);
+                    v += __shfl_xor_sync(0xffffffffu, v, 8);
+                    v += __shfl_xor_sync(0xffffffffu, v, 16);
+                    if (g == 0) colp[rg * kNB + 16 * cp + 8 * j + 2 * t + b] = v;
+                }
+            __syncthreads();
+            for (int r = tid; r < m; r += kThreads) {
+                double s2 = part[r] + part[NMAX + r];
+                if (r < nb) s2 += colp[r] + colp[kNB + r] + colp[2 * kNB + r] + colp[3 * kNB + r];
+                rowsum[k0 + r] += s2;
+            }
+        }
+        // The next panel's columns of A (lower part) start towards L2 while this panel is updated.
+        if (k0 + kNB < n) {
+            int const kn = k0 + kNB, cols = min(kNB, n - kn), lines = (n - kn + 15) / 16;
+            for (int e = tid; e < cols * lines; e += kThreads) {
+                int const c = e / lines, r = kn + (e - c * lines) * 16;
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(A + r + (int64_t)(kn + c) * lda));
+            }
+        }
+        tc_panel_update_dispatch<MAXR>(acc, F, ldf, buf, k0, m);
+        __syncthreads();
+        // Panel to shared memory, column-major with stride NMAX.
+#pragma unroll
+        for (int s = 0; s < RT; ++s)
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    int const r = 16 * (rg + 4 * s) + g + 8 * (e >> 1);
+                    int const c = 16 * cp + 8 * j + 2 * t + (e & 1);
+                    if (r < m && c < nb) buf[c * NMAX + r] = acc[s][j][e];
+                }
+        __syncthreads();
+        cta_panel_finish<float, NMAX>(buf, nb, m, k0, F, ldf, rinv, s_info, blk64);
+    }
+    return *s_info;
+}
+
 // In-place solve with the factor: v := F^{-T} F^{-1} v (v in shared memory, precision T).
 // Blockwise with look-ahead, one barrier per 32-row block: once block b is solved, warp 0 applies
 // it to the next block's 32 entries and solves that block's 32 x 32 triangle from registers
@@ -665,18 +907,38 @@ __global__ void __launch_bounds__(kThreads, MAXR <= 8 ? 2 : 1) posv_cta_f64_kern
     }
 }
 
-// Mixed path: binary32 factor in the workspace, binary64 refinement.
-template <int MAXR, class Batch>
+// Shared-memory layout of the mixed kernel: the panel / staging buffer (binary32, large enough
+// for the tensor-core update's padded staging in modes 1 and 2), four vectors of NMAX doubles plus
+// reductions, and, for binary64 diagonal blocks, a 32 x 32 block of doubles and its 32 reciprocals.
+template <int MAXR, int MODE>
+struct MixedSmem {
+    static constexpr int NMAX = 32 * MAXR;
+    static constexpr bool kTc = MODE == 1 || MODE == 2;
+    static constexpr bool kDiag64 = MODE == 2 || MODE == 3;
+    static constexpr int kBufElems = (kTc && TcShape<MAXR>::kStageElems > Smem<float, MAXR>::kBufElems)
+                                         ? TcShape<MAXR>::kStageElems
+                                         : Smem<float, MAXR>::kBufElems;
+    static constexpr size_t kVecOffset = sizeof(float) * kBufElems;
+    static constexpr size_t kBlkOffset = kVecOffset + sizeof(double) * (4 * NMAX + 64);
+    static constexpr size_t kBytes = kBlkOffset + (kDiag64 ? sizeof(double) * (32 * 32 + 32) : 0);
+};
+
+// Mixed path: binary32 factor in the workspace, binary64 refinement. MODE selects the
+// factorisation: 0 = binary32 CUDA-core panel update (cta_potrf<float>), 1 = tensor-core 3xTF32
+// panel update (cta_potrf_tc), 2 = as 1 with binary64 diagonal blocks, 3 = as 0 with binary64
+// diagonal blocks.
+template <int MAXR, class Batch, int MODE>
 __global__ void __launch_bounds__(kThreads, 2) posv_cta_mixed_kernel(Batch batch, CtaArgs args) {
-    using S = Smem<float, MAXR>;
+    using S = MixedSmem<MAXR, MODE>;
     constexpr int NMAX = S::NMAX;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* buf = reinterpret_cast<float*>(smem_raw);
-    double* x = reinterpret_cast<double*>(smem_raw + sizeof(float) * S::kBufElems);
+    double* x = reinterpret_cast<double*>(smem_raw + S::kVecOffset);
     double* r = x + NMAX;
     double* bb = r + NMAX;
     float* w = reinterpret_cast<float*>(bb + NMAX);  // NMAX floats (fits in the 4th vector)
     double* red = bb + 2 * NMAX;
+    double* blk64 = S::kDiag64 ? reinterpret_cast<double*>(smem_raw + S::kBlkOffset) : nullptr;
     __shared__ int s_info;
     int64_t const b = blockIdx.x;
     if (b >= args.batch) return;
@@ -694,7 +956,9 @@ __global__ void __launch_bounds__(kThreads, 2) posv_cta_mixed_kernel(Batch batch
     for (int i = tid; i < n; i += kThreads) r[i] = 0.0;
     __syncthreads();
     // the factorisation also leaves the row sums of |A| in r
-    int const info = cta_potrf<float, MAXR>(n, it.A, it.lda, F, n, buf, &s_info, r);
+    int info;
+    if constexpr (S::kTc) info = cta_potrf_tc<MAXR>(n, it.A, it.lda, F, n, buf, &s_info, r, blk64);
+    else info = cta_potrf<float, MAXR>(n, it.A, it.lda, F, n, buf, &s_info, r, blk64);
     if (tid == 0 && args.info) args.info[b] = info;
 
     // |A|_inf = max row sum of |A| (accumulated by the factorisation from the lower triangle)
@@ -841,13 +1105,33 @@ int launch_bwd(DescBwd const& batch, int64_t count, int recompute, int32_t* info
     return check_launch();
 }
 
+template <int MAXR, class Batch, int MODE>
+cudaError_t launch_mixed(Batch const& batch, CtaArgs const& args, cudaStream_t s) {
+    size_t const smem = MixedSmem<MAXR, MODE>::kBytes;
+    cudaError_t const e = ensure_smem<posv_cta_mixed_kernel<MAXR, Batch, MODE>>(smem);
+    if (e == cudaSuccess)
+        posv_cta_mixed_kernel<MAXR, Batch, MODE><<<(unsigned)args.batch, kThreads, smem, s>>>(batch, args);
+    return e;
+}
+
+// "posv.mixed.n<bin>" selects the mixed factorisation per size bin (MODE of posv_cta_mixed_kernel;
+// default 0, the fastest measured on GB300).
 template <int MAXR, class Batch>
 int launch_cta(bool mixed, Batch const& batch, CtaArgs const& args, cudaStream_t s) {
-    size_t const smem = mixed ? Smem<float, MAXR>::kBytes : Smem<double, MAXR>::kBytes;
-    cudaError_t e;
+    size_t const smem = Smem<double, MAXR>::kBytes;
+    cudaError_t e = cudaSuccess;
     if (mixed) {
-        e = ensure_smem<posv_cta_mixed_kernel<MAXR, Batch>>(smem);
-        if (e == cudaSuccess) posv_cta_mixed_kernel<MAXR, Batch><<<(unsigned)args.batch, kThreads, smem, s>>>(batch, args);
+        // only descriptor batches carry the mixed path's workspace offsets
+        if constexpr (std::is_same_v<Batch, DescPosv>) {
+            switch (tune_get_bin("posv.mixed", 32 * MAXR, 0)) {
+                case 1: e = launch_mixed<MAXR, Batch, 1>(batch, args, s); break;
+                case 2: e = launch_mixed<MAXR, Batch, 2>(batch, args, s); break;
+                case 3: e = launch_mixed<MAXR, Batch, 3>(batch, args, s); break;
+                default: e = launch_mixed<MAXR, Batch, 0>(batch, args, s); break;
+            }
+        } else {
+            return BLASTGPU_ERR_NOT_IMPLEMENTED;
+        }
     } else {
         e = ensure_smem<posv_cta_f64_kernel<MAXR, Batch>>(smem);
         if (e == cudaSuccess) posv_cta_f64_kernel<MAXR, Batch><<<(unsigned)args.batch, kThreads, smem, s>>>(batch, args);

@@ -91,6 +91,49 @@ def test_ragged_posv_mixed_backward_error(gpu, cond):
         assert _fwd_inf(Xg, np.linalg.solve(Ah, Bh)) <= bound, n
 
 
+@pytest.mark.parametrize("mode", [0, 1, 2, 3])
+def test_ragged_posv_mixed_factorisations(gpu, mode):
+    """Every factorisation of the mixed kernel (0: binary32 CUDA-core panel update, 1: tensor-core
+    3xTF32 update, 2: tensor-core update with binary64 diagonal blocks, 3: CUDA-core update with
+    binary64 diagonal blocks) over every size bin (n <= 64, 128, 256, 512, including sizes that are
+    not multiples of 16 or 32) converges to the backward-error tolerance and agrees with the
+    binary64 path."""
+    import torch
+
+    from blast_gb300 import _lib
+    from blast_gb300.ragged import Packed, PosvPlan
+
+    rng = np.random.default_rng(40 + mode)
+    cond = 1e6
+    ns = [1, 5, 16, 17, 33, 64, 65, 100, 127, 128, 129, 191, 250, 256, 257, 333, 480, 505, 512]
+    As = [_spd_cond(rng, n, cond) for n in ns]
+    Bs = [rng.standard_normal((n, 1)) for n in ns]
+    A = Packed(ns, ns, "cuda")
+    A.fill_from(As)
+    B = Packed(ns, [1] * len(ns), "cuda")
+    B.fill_from(Bs)
+    X, X64, L64 = Packed(ns, [1] * len(ns), "cuda"), Packed(ns, [1] * len(ns), "cuda"), Packed(ns, ns, "cuda")
+    old = _lib.tune_get("posv.mixed")
+    _lib.tune_set("posv.mixed", mode)
+    try:
+        plan = PosvPlan(A, B, X, mixed=True, tol=1e-12, max_iter=20)
+        plan.run()
+        torch.cuda.synchronize()
+    finally:
+        _lib.tune_set("posv.mixed", old if old is not None else 0)
+    PosvPlan(A, B, X64, L64).run()
+    torch.cuda.synchronize()
+    info, iters, berr = plan.results()
+    assert not info.any(), info
+    assert np.all(berr <= 1e-12), (berr, ns)
+    for n, Ah, Bh, Xg, X64g in zip(ns, As, Bs, X.to_list(), X64.to_list()):
+        r = Bh - Ah @ Xg
+        be = np.abs(r).max() / (np.abs(Ah).sum(1).max() * np.abs(Xg).max() + np.abs(Bh).max())
+        assert be <= 1e-12, (n, be)
+        bound = 2.5e-12 * np.linalg.cond(Ah, np.inf)
+        assert _fwd_inf(Xg, X64g) <= bound, (n, _fwd_inf(Xg, X64g), bound)
+
+
 def test_ragged_posv_mixed_reports_breakdown(gpu):
     """A matrix that is not positive definite: the mixed path reports info and a huge backward
     error instead of a solution (the caller re-solves it on the binary64 path)."""
