@@ -176,6 +176,19 @@ def peak_dmma_tflops() -> float:
     return out.value
 
 
+def peak_mma_tflops(kind: int) -> float:
+    """mma.sync throughput (0: TF32 m16n8k8, 1: BF16 m16n8k16) measured by the library's probe kernel."""
+    import ctypes
+
+    import torch
+
+    from blast_gb300 import _lib
+
+    out = ctypes.c_double(0.0)
+    _lib.call("blastgpu_probe_mma_tflops", kind, ctypes.byref(out), torch.cuda.current_stream().cuda_stream)
+    return out.value
+
+
 def _hbm_peak():
     try:
         return json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs")

@@ -51,6 +51,7 @@ SIGNATURES: dict[str, list] = {
     "blastgpu_selftest_recip": [I32, PTR, PTR, I32, PTR],
     "blastgpu_probe_fp64_tflops": [PTR, PTR],
     "blastgpu_probe_fp64_dmma_tflops": [PTR, PTR],
+    "blastgpu_probe_mma_tflops": [I32, PTR, PTR],
     "blastgpu_tune_set": [C.c_char_p, I32],
     "blastgpu_tune_get": [C.c_char_p, PTR],
     "blastgpu_dgemm_strided": [I32, I32, I32, I32, I32, DBL, PTR, I32, I64, PTR, I32, I64, DBL,

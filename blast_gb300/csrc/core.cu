@@ -113,6 +113,41 @@ __global__ void dmma_probe_kernel(int iters, double* sink) {
     sink[threadIdx.x] = s;
 }
 
+// Binary32-accumulating tensor-core throughput probe (mma.sync): KIND 0 = m16n8k8 TF32,
+// KIND 1 = m16n8k16 BF16; CHAINS independent accumulators per warp.
+template <int KIND, int CHAINS>
+__global__ void mma_probe_kernel(int iters, double* sink) {
+    float c[CHAINS][4];
+#pragma unroll
+    for (int q = 0; q < CHAINS; ++q)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) c[q][e] = 0.f;
+    uint32_t const a0 = 0x3c003c00u + threadIdx.x, a1 = a0 + 1u, a2 = a0 + 2u, a3 = a0 + 3u, b0 = 0x3c003c00u;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int q = 0; q < CHAINS; ++q) {
+            if constexpr (KIND == 0)
+                asm volatile(
+                    "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+                    "{%0, %1, %2, %3};\n"
+                    : "+f"(c[q][0]), "+f"(c[q][1]), "+f"(c[q][2]), "+f"(c[q][3])
+                    : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b0));
+            else
+                asm volatile(
+                    "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+                    "{%0, %1, %2, %3};\n"
+                    : "+f"(c[q][0]), "+f"(c[q][1]), "+f"(c[q][2]), "+f"(c[q][3])
+                    : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b0));
+        }
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int q = 0; q < CHAINS; ++q)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) s += c[q][e];
+    sink[threadIdx.x] = s;
+}
+
 constexpr int kProbeMaxThreads = 160 * 8 * 256;
 __device__ double g_probe_out[kProbeMaxThreads];
 __device__ double g_probe_sink[256];
@@ -246,6 +281,44 @@ int blastgpu_probe_fp64_dmma_tflops(double* tflops, blastgpu_stream_t stream) {
             double const tf = 512.0 * chains * (double)iters * warps / (ms * 1e-3) / 1e12;
             if (rep > 0 && tf > best) best = tf;
         }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
+    *tflops = best;
+    return BLASTGPU_SUCCESS;
+}
+
+// Diagnostic export: throughput (TFLOP/s) of the warp-level tensor-core instruction the mixed
+// path's tensor-core update uses (kind 0: mma.sync m16n8k8 TF32) or its BF16 counterpart
+// (kind 1: m16n8k16), binary32 accumulation; synchronises the stream.
+int blastgpu_probe_mma_tflops(int kind, double* tflops, blastgpu_stream_t stream) {
+    if (kind != 0 && kind != 1) return -1;
+    if (!tflops) return -2;
+    cudaStream_t const s = as_cuda(stream);
+    double* sink = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void**>(&sink), g_probe_sink);
+    if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
+    int const threads = 256, blocks = sm_count() * 2, iters = 4096, chains = 8;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    double best = 0.0;
+    for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
+        cudaEventRecord(e0, s);
+        if (kind == 0) mma_probe_kernel<0, 8><<<blocks, threads, 0, s>>>(iters, sink);
+        else mma_probe_kernel<1, 8><<<blocks, threads, 0, s>>>(iters, sink);
+        cudaEventRecord(e1, s);
+        e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        double const k = kind == 0 ? 8.0 : 16.0;
+        double const warps = (double)blocks * threads / 32;
+        double const tf = 2.0 * 16 * 8 * k * chains * (double)iters * warps / (ms * 1e-3) / 1e12;
+        if (rep > 0 && tf > best) best = tf;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -9,11 +9,15 @@ Tunable choices (read by the library through blastgpu_tune_set / tune_get_bin):
   per largest dimension rounded up to a multiple of 8.
 * ``getrf.cta.n<bin>`` — ragged LU: one warp (0) or one 256-thread CTA (1) per matrix, per size bin
   of the launch's largest n (same bits either way).
+* ``getrf.lazy.n<bin>`` — the CTA kernel's schedule: right-looking (0) or left-looking with the left
+  row swaps deferred (1); same bits either way.
 * ``posv.mixed.n<bin>`` — ragged mixed-precision Cholesky factorisation per size bin (the modes of
   posv_cta_mixed_kernel); timed on the mixed workload's matrices (cond 1e2, 1e4, 1e6) and kept only
   if every instance converges.
 * ``posv.cta_min_n`` — uniform Cholesky batches from this n on run one CTA per matrix instead of one
   thread per matrix.
+* ``posv.persistent`` — the CTA-per-matrix Cholesky kernels launch one CTA per instance (0) or only
+  as many CTAs as the SMs hold, each looping over instances (1); same bits either way.
 
 Results are cached as JSON keyed by GPU name (``blast_gb300/tuning/<gpu>.json``); ``apply()``
 loads the cache for the current GPU into the library, and ``import blast_gb300`` calls it.
@@ -127,7 +131,8 @@ def _log_uniform_sizes(rng, lo: int, hi: int, count: int):
 
 
 def tune_getrf(bins=(8, 16, 32, 64, 128, 256), count: int = 4000) -> dict:
-    """Warp- or CTA-per-matrix LU per size bin, on ragged batches with n log-uniform in the bin."""
+    """Warp-per-matrix LU, or CTA-per-matrix LU right- or left-looking, per size bin, on ragged
+    batches with n log-uniform in the bin."""
     import numpy as np
 
     from .ragged import GesvPlan, Packed
@@ -141,9 +146,11 @@ def tune_getrf(bins=(8, 16, 32, 64, 128, 256), count: int = 4000) -> dict:
         A0 = torch.randn(A.buf.numel(), device="cuda", dtype=torch.float64)
         plan = GesvPlan(A, B)
         key = f"getrf.cta.n{size_bin(int(ns.max()))}"
+        lazy_key = f"getrf.lazy.n{size_bin(int(ns.max()))}"
         times = {}
-        for v in (0, 1):
-            _lib.tune_set(key, v)
+        for v in ((0, 0), (1, 0), (1, 1)):
+            _lib.tune_set(key, v[0])
+            _lib.tune_set(lazy_key, v[1])
 
             def step():
                 A.buf.copy_(A0)
@@ -151,12 +158,14 @@ def tune_getrf(bins=(8, 16, 32, 64, 128, 256), count: int = 4000) -> dict:
                           int(ns.max()), torch.cuda.current_stream().cuda_stream)
 
             times[v] = _time(step, reps=5)
-        out[key] = min(times, key=times.get)
-        _lib.tune_set(key, out[key])
+        best = min(times, key=times.get)
+        out[key], out[lazy_key] = best
+        _lib.tune_set(key, best[0])
+        _lib.tune_set(lazy_key, best[1])
     return out
 
 
-def tune_posv_mixed(bins=(64, 128, 256, 512), count: int = 1536, modes=(0, 1, 2)) -> dict:
+def tune_posv_mixed(bins=(64, 128, 256, 512), count: int = 1536, modes=(0, 1, 2, 3)) -> dict:
     """Mixed-precision factorisation per size bin, on SPD matrices with n uniform in the bin and
     cond(A) in {1e2, 1e4, 1e6}; a mode counts only if every instance converges."""
     import numpy as np
@@ -223,6 +232,36 @@ def tune_posv_cta_min_n(ns=(48, 56, 64, 72, 80, 96, 112, 128), nrhs=8, batch=20_
     return {"posv.cta_min_n": int(value)}
 
 
+def tune_posv_persistent(count: int = 8192) -> dict:
+    """One CTA per instance or a persistent grid, timed on the mixed workload's ragged batch
+    (n ~ U{64..512}, both the binary64 and the mixed path)."""
+    import numpy as np
+
+    from .ragged import Packed, PosvPlan
+
+    rng = np.random.default_rng(6)
+    ns = rng.integers(64, 513, count)
+    A = Packed(ns, ns, "cuda")
+    for n in np.unique(ns):
+        idx = np.nonzero(ns == n)[0]
+        G = torch.randn(len(idx), int(n), int(n), device="cuda", dtype=torch.float64)
+        M = G @ G.mT / int(n) + torch.eye(int(n), device="cuda", dtype=torch.float64)
+        for j, i in enumerate(idx):
+            A.view(int(i)).copy_(M[j])
+    ones = np.ones_like(ns)
+    B, X = Packed(ns, ones, "cuda"), Packed(ns, ones, "cuda")
+    B.buf.copy_(torch.randn(B.buf.numel(), device="cuda", dtype=torch.float64))
+    L = Packed(ns, ns, "cuda")
+    plans = (PosvPlan(A, B, X, L), PosvPlan(A, B, X, mixed=True, tol=1e-12, max_iter=10))
+    times = {}
+    for v in (0, 1):
+        _lib.tune_set("posv.persistent", v)
+        times[v] = sum(_time(p.run, reps=3) for p in plans)
+    best = min(times, key=times.get)
+    _lib.tune_set("posv.persistent", best)
+    return {"posv.persistent": int(best)}
+
+
 def run(save: bool = True) -> dict:
     """Tunes every choice on the current GPU and (optionally) writes the cache."""
     choices = {}
@@ -231,6 +270,7 @@ def run(save: bool = True) -> dict:
     choices.update(tune_getrf())
     choices.update(tune_posv_mixed())
     choices.update(tune_posv_cta_min_n())
+    choices.update(tune_posv_persistent())
     if save:
         CACHE_DIR.mkdir(parents=True, exist_ok=True)
         cache_path().write_text(json.dumps({"gpu": torch.cuda.get_device_name(),

@@ -93,6 +93,10 @@ int blastgpu_probe_fp64_tflops(double* tflops, blastgpu_stream_t stream);
 /* probe_fp64_dmma_tflops: the same measurement for the binary64 tensor-core instruction
  * (mma.sync m8n8k4 f64), so that its rate can be compared with the FMA pipe's on the same GPU. */
 int blastgpu_probe_fp64_dmma_tflops(double* tflops, blastgpu_stream_t stream);
+/* probe_mma_tflops: the same for the warp-level tensor-core instruction of the mixed path's
+ * tensor-core panel update (kind 0: mma.sync m16n8k8 TF32) and its BF16 counterpart (kind 1:
+ * m16n8k16), binary32 accumulation. */
+int blastgpu_probe_mma_tflops(int kind, double* tflops, blastgpu_stream_t stream);
 
 /* blastgpu_dposv_strided for operands outside device memory: A and B are read in place and L and
  * X written in place, each element once, from/to any memory the GPU can address (pinned host

@@ -220,21 +220,24 @@ def test_getrs_large_n_bitexact(gpu, oracle_lib, n):
 
 
 def test_getrf_kernel_choice_keeps_bits(gpu, oracle_lib):
-    """The autotuner's per-bin choice between the warp-per-matrix and CTA-per-matrix LU kernels
-    ("getrf.cta.n<bin>") changes the schedule, never the result: factors and pivots are identical
-    under both choices and equal to the oracle's."""
+    """The autotuner's per-bin choices between the warp-per-matrix LU kernel, the CTA kernel's
+    right-looking schedule and its left-looking schedule ("getrf.cta.n<bin>", "getrf.lazy.n<bin>")
+    change the schedule, never the result: factors, pivots and solutions are identical under every
+    choice and equal to the oracle's."""
     import torch
 
     from blast_gb300 import _lib
     from blast_gb300.ragged import GesvPlan, Packed
 
     rng = np.random.default_rng(91)
-    ns = [7, 40, 65, 100, 129, 200, 256, 31]
+    ns = [7, 40, 65, 100, 129, 200, 256, 31, 1, 4, 5, 8, 9, 33, 67, 97, 130, 255, 300, 512]
     mats = [rng.standard_normal((n, n)) for n in ns]
+    bins = (8, 16, 32, 64, 128, 256, 512)
     results = []
-    for choice in (0, 1):
-        for b in (8, 16, 32, 64, 128, 256):
-            _lib.tune_set(f"getrf.cta.n{b}", choice)
+    for cta, lazy in ((0, 0), (1, 0), (1, 1)):
+        for b in bins:
+            _lib.tune_set(f"getrf.cta.n{b}", cta)
+            _lib.tune_set(f"getrf.lazy.n{b}", lazy)
         try:
             A = Packed(ns, ns, "cuda")
             A.fill_from(mats)
@@ -243,14 +246,51 @@ def test_getrf_kernel_choice_keeps_bits(gpu, oracle_lib):
             plan = GesvPlan(A, B)
             plan.run()
             torch.cuda.synchronize()
-            results.append((A.to_list(), plan.pivots(), B.to_list()))
+            results.append((A.to_list(), plan.pivots(), B.to_list(), plan.info_host()))
         finally:
-            for b in (8, 16, 32, 64, 128, 256):
+            for b in bins:
                 _lib.tune_set(f"getrf.cta.n{b}", 1 if b > 64 else 0)
-    (LU0, P0, X0), (LU1, P1, X1) = results
+                _lib.tune_set(f"getrf.lazy.n{b}", 0)
+    LU0, P0, X0, I0 = results[0]
+    assert not I0.any()
+    for LU1, P1, X1, I1 in results[1:]:
+        for i, n in enumerate(ns):
+            assert np.array_equal(LU0[i], LU1[i]) and np.array_equal(P0[i], P1[i]), n
+            assert np.array_equal(X0[i], X1[i]) and I0[i] == I1[i], n
     for i, n in enumerate(ns):
-        assert np.array_equal(LU0[i], LU1[i]) and np.array_equal(P0[i], P1[i]) and np.array_equal(X0[i], X1[i])
         LUr = np.asfortranarray(mats[i].copy())
         pr = np.zeros(n, dtype=np.int32)
         oracle_lib.getrf(LUr, pr)
-        assert np.array_equal(LU0[i], LUr) and np.array_equal(P0[i], pr)
+        assert np.array_equal(LU0[i], LUr) and np.array_equal(P0[i], pr), n
+
+
+def test_getrf_left_looking_singular_and_ties(gpu, oracle_lib):
+    """The left-looking schedule on matrices with exact pivot ties (BLAST's strict '>' keeps the
+    first) and with an exactly singular column: factors and pivots equal the oracle's, and a
+    singular instance reports the oracle's first zero pivot."""
+    import torch
+
+    from blast_gb300.ragged import GesvPlan, Packed
+
+    rng = np.random.default_rng(92)
+    n = 150
+    tie = np.round(rng.standard_normal((n, n)) * 4) / 4  # many exactly equal magnitudes
+    sing = rng.standard_normal((n, n))
+    sing[:, 77] = 0.0
+    ns = [n, n]
+    A = Packed(ns, ns, "cuda")
+    A.fill_from([tie, sing])
+    B = Packed(ns, [1, 1], "cuda")
+    B.fill_from([np.ones((n, 1)), np.ones((n, 1))])
+    plan = GesvPlan(A, B)
+    plan.run()
+    torch.cuda.synchronize()
+    info = plan.info_host()
+    LUr = np.asfortranarray(tie.copy())
+    pr = np.zeros(n, dtype=np.int32)
+    assert oracle_lib.getrf(LUr, pr) == 0
+    assert info[0] == 0
+    assert np.array_equal(A.to_list()[0], LUr) and np.array_equal(plan.pivots()[0], pr)
+    LUs = np.asfortranarray(sing.copy())
+    ps = np.zeros(n, dtype=np.int32)
+    assert info[1] == oracle_lib.getrf(LUs, ps) == 78
