@@ -166,8 +166,16 @@ __device__ __forceinline__ void panel_update(T (&acc)[MAXR][4], const T* F, int 
         for (int q = 0; q < kc; ++q) {
             T const* col = base + q * NMAX;
             T b[4];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) b[j] = col[c0 + j];
+            // the warp's 4 panel columns in one (binary32) or two (binary64) 16-byte broadcast
+            // loads: NMAX and c0 are multiples of 4 elements and the buffer is 16-byte aligned
+            if constexpr (sizeof(T) == 4) {
+                float4 const v = *reinterpret_cast<float4 const*>(col + c0);
+                b[0] = v.x, b[1] = v.y, b[2] = v.z, b[3] = v.w;
+            } else {
+                double2 const v0 = *reinterpret_cast<double2 const*>(col + c0);
+                double2 const v1 = *reinterpret_cast<double2 const*>(col + c0 + 2);
+                b[0] = v0.x, b[1] = v0.y, b[2] = v1.x, b[3] = v1.y;
+            }
 #pragma unroll
             for (int i = 0; i < RA; ++i) {
                 T const a = col[lane + 32 * i];
@@ -884,12 +892,14 @@ struct CtaArgs {
 
 // Plain binary64 path: factor into L, then X = A^{-1} B column by column.
 template <int MAXR, class Batch>
-__device__ __forceinline__ void posv_cta_f64_item(Batch const& batch, CtaArgs const& args, int64_t b) {
+__global__ void __launch_bounds__(kThreads, MAXR <= 8 ? 2 : 1) posv_cta_f64_kernel(Batch batch, CtaArgs args) {
     using S = Smem<double, MAXR>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double* buf = reinterpret_cast<double*>(smem_raw);
     double* vec = buf + S::kBufElems;
     __shared__ int s_info;
+    int64_t const b = blockIdx.x;
+    if (b >= args.batch) return;
     CtaItem const it = batch.get(b);
     int const n = it.n;
     if (it.A != nullptr) {  // A == nullptr: solves with the given factor L only
@@ -901,17 +911,6 @@ __device__ __forceinline__ void posv_cta_f64_item(Batch const& batch, CtaArgs co
         __syncthreads();
         cta_potrs<double, MAXR>(n, it.L, it.ldl, vec);
         for (int i = threadIdx.x; i < n; i += kThreads) it.X[i + (int64_t)c * it.ldx] = vec[i];
-        __syncthreads();
-    }
-}
-
-// One CTA per matrix. Launched with one CTA per instance, or persistently (grid = the CTAs the
-// SMs hold at once), each CTA then taking instances b, b + gridDim.x, ... of the largest-first
-// order, which deals every CTA a similar mix of sizes.
-template <int MAXR, class Batch>
-__global__ void __launch_bounds__(kThreads, MAXR <= 8 ? 2 : 1) posv_cta_f64_kernel(Batch batch, CtaArgs args) {
-    for (int64_t b = blockIdx.x; b < args.batch; b += gridDim.x) {
-        posv_cta_f64_item<MAXR>(batch, args, b);
         __syncthreads();
     }
 }
@@ -937,7 +936,7 @@ struct MixedSmem {
 // panel update (cta_potrf_tc), 2 = as 1 with binary64 diagonal blocks, 3 = as 0 with binary64
 // diagonal blocks.
 template <int MAXR, class Batch, int MODE>
-__device__ __forceinline__ void posv_cta_mixed_item(Batch const& batch, CtaArgs const& args, int64_t b) {
+__global__ void __launch_bounds__(kThreads, 2) posv_cta_mixed_kernel(Batch batch, CtaArgs args) {
     using S = MixedSmem<MAXR, MODE>;
     constexpr int NMAX = S::NMAX;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -949,6 +948,8 @@ __device__ __forceinline__ void posv_cta_mixed_item(Batch const& batch, CtaArgs 
     double* red = bb + 2 * NMAX;
     double* blk64 = S::kDiag64 ? reinterpret_cast<double*>(smem_raw + S::kBlkOffset) : nullptr;
     __shared__ int s_info;
+    int64_t const b = blockIdx.x;
+    if (b >= args.batch) return;
     CtaItem const it = batch.get(b);
     int const n = it.n, tid = threadIdx.x;
     if (n < 0) {  // scratch range outside the fixed array: reported, nothing written
@@ -1025,14 +1026,6 @@ __device__ __forceinline__ void posv_cta_mixed_item(Batch const& batch, CtaArgs 
     if (tid == 0) {
         if (args.iters) args.iters[b] = total_iters;
         if (args.berr) args.berr[b] = worst;
-    }
-}
-
-template <int MAXR, class Batch, int MODE>
-__global__ void __launch_bounds__(kThreads, 2) posv_cta_mixed_kernel(Batch batch, CtaArgs args) {
-    for (int64_t b = blockIdx.x; b < args.batch; b += gridDim.x) {
-        posv_cta_mixed_item<MAXR, Batch, MODE>(batch, args, b);
-        __syncthreads();
     }
 }
 
@@ -1120,27 +1113,12 @@ int launch_bwd(DescBwd const& batch, int64_t count, int recompute, int32_t* info
     return check_launch();
 }
 
-// Grid of a CTA-per-matrix launch: one CTA per instance, or with "posv.persistent" = 1 only as
-// many as the SMs hold at once (each then loops over instances).
-template <auto Kernel>
-cudaError_t cta_grid(int64_t batch, size_t smem, unsigned& grid) {
-    grid = (unsigned)batch;
-    if (tune_get("posv.persistent", 0) == 0) return cudaSuccess;
-    int per_sm = 0;
-    cudaError_t const e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, Kernel, kThreads, smem);
-    if (e != cudaSuccess) return e;
-    int64_t const resident = (int64_t)(per_sm > 0 ? per_sm : 1) * sm_count();
-    if (resident < batch) grid = (unsigned)resident;
-    return cudaSuccess;
-}
-
 template <int MAXR, class Batch, int MODE>
 cudaError_t launch_mixed(Batch const& batch, CtaArgs const& args, cudaStream_t s) {
     size_t const smem = MixedSmem<MAXR, MODE>::kBytes;
-    cudaError_t e = ensure_smem<posv_cta_mixed_kernel<MAXR, Batch, MODE>>(smem);
-    unsigned grid = 0;
-    if (e == cudaSuccess) e = cta_grid<posv_cta_mixed_kernel<MAXR, Batch, MODE>>(args.batch, smem, grid);
-    if (e == cudaSuccess) posv_cta_mixed_kernel<MAXR, Batch, MODE><<<grid, kThreads, smem, s>>>(batch, args);
+    cudaError_t const e = ensure_smem<posv_cta_mixed_kernel<MAXR, Batch, MODE>>(smem);
+    if (e == cudaSuccess)
+        posv_cta_mixed_kernel<MAXR, Batch, MODE><<<(unsigned)args.batch, kThreads, smem, s>>>(batch, args);
     return e;
 }
 
@@ -1164,9 +1142,7 @@ int launch_cta(bool mixed, Batch const& batch, CtaArgs const& args, cudaStream_t
         }
     } else {
         e = ensure_smem<posv_cta_f64_kernel<MAXR, Batch>>(smem);
-        unsigned grid = 0;
-        if (e == cudaSuccess) e = cta_grid<posv_cta_f64_kernel<MAXR, Batch>>(args.batch, smem, grid);
-        if (e == cudaSuccess) posv_cta_f64_kernel<MAXR, Batch><<<grid, kThreads, smem, s>>>(batch, args);
+        if (e == cudaSuccess) posv_cta_f64_kernel<MAXR, Batch><<<(unsigned)args.batch, kThreads, smem, s>>>(batch, args);
     }
     if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
     return check_launch();

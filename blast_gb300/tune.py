@@ -16,8 +16,6 @@ Tunable choices (read by the library through blastgpu_tune_set / tune_get_bin):
   if every instance converges.
 * ``posv.cta_min_n`` — uniform Cholesky batches from this n on run one CTA per matrix instead of one
   thread per matrix.
-* ``posv.persistent`` — the CTA-per-matrix Cholesky kernels launch one CTA per instance (0) or only
-  as many CTAs as the SMs hold, each looping over instances (1); same bits either way.
 
 Results are cached as JSON keyed by GPU name (``blast_gb300/tuning/<gpu>.json``); ``apply()``
 loads the cache for the current GPU into the library, and ``import blast_gb300`` calls it.
@@ -232,36 +230,6 @@ def tune_posv_cta_min_n(ns=(48, 56, 64, 72, 80, 96, 112, 128), nrhs=8, batch=20_
     return {"posv.cta_min_n": int(value)}
 
 
-def tune_posv_persistent(count: int = 8192) -> dict:
-    """One CTA per instance or a persistent grid, timed on the mixed workload's ragged batch
-    (n ~ U{64..512}, both the binary64 and the mixed path)."""
-    import numpy as np
-
-    from .ragged import Packed, PosvPlan
-
-    rng = np.random.default_rng(6)
-    ns = rng.integers(64, 513, count)
-    A = Packed(ns, ns, "cuda")
-    for n in np.unique(ns):
-        idx = np.nonzero(ns == n)[0]
-        G = torch.randn(len(idx), int(n), int(n), device="cuda", dtype=torch.float64)
-        M = G @ G.mT / int(n) + torch.eye(int(n), device="cuda", dtype=torch.float64)
-        for j, i in enumerate(idx):
-            A.view(int(i)).copy_(M[j])
-    ones = np.ones_like(ns)
-    B, X = Packed(ns, ones, "cuda"), Packed(ns, ones, "cuda")
-    B.buf.copy_(torch.randn(B.buf.numel(), device="cuda", dtype=torch.float64))
-    L = Packed(ns, ns, "cuda")
-    plans = (PosvPlan(A, B, X, L), PosvPlan(A, B, X, mixed=True, tol=1e-12, max_iter=10))
-    times = {}
-    for v in (0, 1):
-        _lib.tune_set("posv.persistent", v)
-        times[v] = sum(_time(p.run, reps=3) for p in plans)
-    best = min(times, key=times.get)
-    _lib.tune_set("posv.persistent", best)
-    return {"posv.persistent": int(best)}
-
-
 def run(save: bool = True) -> dict:
     """Tunes every choice on the current GPU and (optionally) writes the cache."""
     choices = {}
@@ -270,7 +238,6 @@ def run(save: bool = True) -> dict:
     choices.update(tune_getrf())
     choices.update(tune_posv_mixed())
     choices.update(tune_posv_cta_min_n())
-    choices.update(tune_posv_persistent())
     if save:
         CACHE_DIR.mkdir(parents=True, exist_ok=True)
         cache_path().write_text(json.dumps({"gpu": torch.cuda.get_device_name(),

@@ -203,38 +203,3 @@ def test_ragged_plans_replay_in_cuda_graph(gpu, oracle_lib):
         xr = np.asfortranarray(b.copy())
         oracle_lib.getrs(LUr, pr, xr, xr)
         assert np.array_equal(p, pr) and np.array_equal(x, xr)
-
-
-def test_persistent_launch_gives_the_same_bits(gpu):
-    """"posv.persistent" = 1 launches only as many CTAs as the SMs hold at once, each looping over
-    instances in the plan's largest-first order; every instance is computed by the same code, so
-    the binary64 and mixed results are bit-identical to the one-CTA-per-instance launch."""
-    import torch
-
-    from blast_gb300 import _lib
-    from blast_gb300.ragged import Packed, PosvPlan
-
-    rng = np.random.default_rng(77)
-    ns = list(rng.integers(1, 513, 700))
-    As = [_spd_cond(rng, int(n), 1e4) for n in ns]
-    A = Packed(ns, ns, "cuda")
-    A.fill_from(As)
-    B = Packed(ns, [1] * len(ns), "cuda")
-    B.fill_from([rng.standard_normal((int(n), 1)) for n in ns])
-    out = []
-    for persistent in (0, 1):
-        _lib.tune_set("posv.persistent", persistent)
-        try:
-            X64, L64, X32 = Packed(ns, [1] * len(ns), "cuda"), Packed(ns, ns, "cuda"), Packed(ns, [1] * len(ns), "cuda")
-            p64 = PosvPlan(A, B, X64, L64)
-            pmx = PosvPlan(A, B, X32, mixed=True, tol=1e-12, max_iter=10)
-            p64.run()
-            pmx.run()
-            torch.cuda.synchronize()
-            out.append((X64.buf.clone(), L64.buf.clone(), X32.buf.clone(), pmx.results()))
-        finally:
-            _lib.tune_set("posv.persistent", 0)
-    (x0, l0, m0, r0), (x1, l1, m1, r1) = out
-    assert torch.equal(x0, x1) and torch.equal(l0, l1) and torch.equal(m0, m1)
-    assert all(np.array_equal(a, b) for a, b in zip(r0, r1))
-    assert not r0[0].any() and np.all(r0[2] <= 1e-12)
