@@ -796,20 +796,31 @@ def run_ours(args):
     hB.copy_(B)
     hL, hX = pinned_col_major(BATCH, N, N), pinned_col_major(BATCH, N, NRHS)
     hinfo = torch.empty(BATCH, dtype=torch.int32, pin_memory=True)
+    X_device_path = X.cpu()  # the device-timed solutions, to check every e2e output against
     del A, B, L, X
     torch.cuda.empty_cache()
     chunks = max(1, args.e2e_chunks)
-    e2e_steps = max(2, min(args.steps, 10))
+    e2e_steps = max(3, min(args.steps, 12))
+    depth = max(1, args.e2e_depth)
+    # batches in flight together write to output buffers of their own
+    outs = [(hL, hX, hinfo)] + [(pinned_col_major(BATCH, N, N), pinned_col_major(BATCH, N, NRHS),
+                                 torch.empty(BATCH, dtype=torch.int32, pin_memory=True))
+                                for _ in range(depth - 1)]
     e2e_runs = {}
-    for transport, nchunks in (("copy", chunks), ("direct", 1), ("mirror", 1)):
-        pipe = PosvHostPipeline(N, NRHS, (BATCH + nchunks - 1) // nchunks, dev, transport=transport)
-        for _ in range(2):
-            pipe.run(hA, hB, hL, hX, hinfo)
+    variants = [("copy", "copy", chunks, 1), ("direct", "direct", 1, 1), ("mirror", "mirror", 1, 1)]
+    if depth > 1:
+        variants.append((f"mirror_depth{depth}", "mirror", 1, depth))
+    for name, transport, nchunks, dpt in variants:
+        pipe = PosvHostPipeline(N, NRHS, (BATCH + nchunks - 1) // nchunks, dev, transport=transport, depth=dpt)
+        for i in range(2 * dpt):
+            pipe.run(hA, hB, *outs[i % dpt])
+        pipe.wait()
         torch.cuda.synchronize()
         barrier()
         e0.record(stream)
-        for _ in range(e2e_steps):
-            pipe.run(hA, hB, hL, hX, hinfo)
+        for i in range(e2e_steps):
+            pipe.run(hA, hB, *outs[i % dpt])
+        pipe.wait()
         e1.record(stream)
         torch.cuda.synchronize()
         t_ms = e0.elapsed_time(e1) / e2e_steps
@@ -817,15 +828,18 @@ def run_ours(args):
             t = torch.tensor([t_ms], device=dev)
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             t_ms = float(t.item())
-        e2e_runs[transport] = (t_ms, nchunks)
+        ok = all(int(outs[i][2].abs().sum()) == 0 and bool(torch.equal(outs[i][1], X_device_path))
+                 for i in range(dpt))
+        e2e_runs[name] = (t_ms, nchunks, dpt, ok)
         del pipe
         torch.cuda.empty_cache()
     best = min(e2e_runs, key=lambda k: e2e_runs[k][0])
-    e2e_ms, e2e_chunks = e2e_runs[best]
+    e2e_ms, e2e_chunks, e2e_depth, e2e_same = e2e_runs[best]
+    del X_device_path
     # bytes that cross the host link per step: the mirror kernel reads only lower(A) and writes
     # only lower(L); the copy transports move whole matrices
     tri = N * (N + 1) // 2
-    if best == "mirror":
+    if best.startswith("mirror"):
         h2d = BATCH * (tri + N * NRHS) * 8
         d2h = BATCH * (tri + N * NRHS) * 8 + BATCH * 4
     elif best == "direct":
@@ -834,7 +848,7 @@ def run_ours(args):
     else:
         h2d = hA.numel() * 8 + hB.numel() * 8
         d2h = hL.numel() * 8 + hX.numel() * 8 + BATCH * 4
-    e2e_ok = bool(int(hinfo.abs().sum()) == 0)
+    e2e_ok = all(int(o[2].abs().sum()) == 0 for o in outs)
 
     if rank != 0:
         if ws > 1:
@@ -866,9 +880,13 @@ def run_ours(args):
         "parity": parity,
         "e2e": {"value": ws * BATCH / (e2e_ms * 1e-3), "unit": "matrices/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": e2e_ms, "chunks": e2e_chunks, "info_all_zero": e2e_ok,
-                "path": f"blast_gb300.host.PosvHostPipeline(transport='{best}'), pinned host buffers",
-                "other_transports": [{"transport": t, "ms_per_step": v[0], "chunks": v[1],
+                "ms_per_step": e2e_ms, "chunks": e2e_chunks, "depth": e2e_depth, "info_all_zero": e2e_ok,
+                "x_bitwise_equal_to_device_path": e2e_same,
+                "x_bitwise_equal_all_transports": all(v[3] for v in e2e_runs.values()),
+                "path": f"blast_gb300.host.PosvHostPipeline(transport='{best.split('_')[0]}', depth={e2e_depth}), "
+                        "pinned host buffers" + (f", {e2e_depth} batches in flight, each with its own output "
+                                                 "buffers" if e2e_depth > 1 else ""),
+                "other_transports": [{"transport": t, "ms_per_step": v[0], "chunks": v[1], "depth": v[2],
                                       "value": ws * BATCH / (v[0] * 1e-3)}
                                      for t, v in e2e_runs.items() if t != best]},
         "gpu_launches": launches,
@@ -909,7 +927,9 @@ def run_mixed_only(args):
     if args.mixed_mode is not None:
         from blast_gb300 import _lib
 
-        _lib.tune_set("posv.mixed", args.mixed_mode)
+        # the per-bin keys (set by the tuning cache) take precedence over the global one
+        for key in ("posv.mixed", "posv.mixed.n64", "posv.mixed.n128", "posv.mixed.n256", "posv.mixed.n512"):
+            _lib.tune_set(key, args.mixed_mode)
     print(json.dumps(mixed_ir_comparison(max(1, args.steps), args.mixed_count, args.mixed_gen,
                                          parity=not args.no_parity)), flush=True)
 
@@ -934,6 +954,8 @@ def main():
                     "others print one JSON object for that workload alone")
     ap.add_argument("--count", type=int, default=0,
                     help="instances for --workload lu_ragged / riccati (smaller for profiling)")
+    ap.add_argument("--e2e-depth", type=int, default=3,
+                    help="batches in flight for the pipelined mirror transport (1: not timed)")
     ap.add_argument("--e2e-chunks", type=int, default=3,
                     help="chunks of the staged-copy transport in the end-to-end leg")
     ap.add_argument("--only-mixed", action="store_true",
@@ -943,6 +965,8 @@ def main():
                     help="mixed factorisation for --only-mixed: 0 binary32 CUDA cores, 1 tensor cores "
                          "(3xTF32), 2 tensor cores with binary64 diagonal blocks, 3 CUDA cores with "
                          "binary64 diagonal blocks (default: the library's)")
+    ap.add_argument("--getrf-lazy", type=int, choices=[0, 1], default=None,
+                    help="lu_ragged: right-looking (0) or left-looking (1) CTA LU in every size bin")
     ap.add_argument("--mixed-gen", choices=["qr", "gram"], default="qr",
                     help="qr: the workload's Q diag(lambda) Q^T matrices; gram: G G^T/n + I, for "
                          "profilers under which torch.linalg cannot load")
@@ -955,6 +979,11 @@ def main():
         if args.workload == "gemm24":
             res = config_gemm24(args.steps, peak, cpu=not args.no_cpu)
         elif args.workload == "lu_ragged":
+            if args.getrf_lazy is not None:
+                from blast_gb300 import _lib
+
+                for b in (8, 16, 32, 64, 128, 256, 512):
+                    _lib.tune_set(f"getrf.lazy.n{b}", args.getrf_lazy)
             res = config_lu_ragged(args.steps, peak, count=args.count or 20_000, cpu=not args.no_cpu)
         elif args.workload == "adjoint":
             res = config_adjoint(args.steps, peak)

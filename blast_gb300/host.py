@@ -10,7 +10,11 @@ as BLAST's do. Three transports:
   reads cross NVLink-C2C as it computes, so only the result direction is staged.
 * ``"mirror"``: one launch (blastgpu_dposv_mirror_strided); the kernel reads the host inputs
   directly and each warp, once its 32 instances are solved, writes their L and X to the host
-  buffers with whole-line stores, while other warps compute.
+  buffers with whole-line stores, while other warps compute. With ``depth`` > 1, up to ``depth``
+  batches are in flight at once, each on a stream and a device workspace of its own: the next
+  batch's warps start reading their inputs over the host link while the previous batch's warps
+  still compute, so the link and the binary64 pipes stay busy together (every warp of one launch
+  asks for its next strip at about the same moment, which leaves the link idle while they compute).
 
 Device buffers are allocated once per pipeline and reused.
 """
@@ -40,15 +44,21 @@ class PosvHostPipeline:
     column-major per matrix (a (batch, n, n) tensor whose .mT is contiguous, as made by
     pinned_col_major)."""
 
-    def __init__(self, n: int, nrhs: int, chunk: int, device=None, transport: str = "copy"):
+    def __init__(self, n: int, nrhs: int, chunk: int, device=None, transport: str = "copy", depth: int = 1):
         if transport not in TRANSPORTS:
             raise ValueError(f"transport must be one of {TRANSPORTS}")
-        self.n, self.nrhs, self.chunk, self.transport = n, nrhs, chunk, transport
+        if depth < 1 or (depth > 1 and transport != "mirror"):
+            raise ValueError("depth > 1 needs the mirror transport")
+        self.n, self.nrhs, self.chunk, self.transport, self.depth = n, nrhs, chunk, transport, depth
         self.device = torch.device(device or "cuda")
         self.info = torch.zeros(0, dtype=torch.int32, device=self.device)
         if transport == "mirror":
-            self.wL = torch.empty((chunk, n, n), dtype=torch.float64, device=self.device)
-            self.wX = torch.empty((chunk, max(nrhs, 1), n), dtype=torch.float64, device=self.device)
+            self.work = [(torch.empty((chunk, n, n), dtype=torch.float64, device=self.device),
+                          torch.empty((chunk, max(nrhs, 1), n), dtype=torch.float64, device=self.device))
+                         for _ in range(depth)]
+            self.slot_streams = [torch.cuda.Stream(self.device) for _ in range(depth)] if depth > 1 else []
+            self.slot_info = [self.info] * depth
+            self.next_slot = 0
             return
         self.streams = [torch.cuda.Stream(self.device) for _ in range(_SLOTS)]
         self.dL = [col_major((chunk,), n, n, self.device) for _ in range(_SLOTS)]
@@ -64,12 +74,31 @@ class PosvHostPipeline:
             hinfo: torch.Tensor | None = None) -> torch.Tensor:
         """Enqueues the whole batch; returns the device info array (also copied to the pinned
         int32 host tensor hinfo when given). Host outputs are complete once
-        torch.cuda.current_stream() has passed the point of return (it waits on the pipeline)."""
+        torch.cuda.current_stream() has passed the point of return (it waits on the pipeline).
+
+        With depth > 1 the batch runs on the next of the pipeline's own streams, after the work
+        enqueued so far on the current stream, and the current stream does not wait for it: the
+        outputs are complete once the current stream has passed a later wait(). Until then the
+        batch's host buffers must stay untouched, and batches in flight together need output
+        buffers (hL, hX, hinfo) of their own."""
         batch = hA.shape[0]
+        if self.transport == "mirror" and self.depth > 1:
+            slot = self.next_slot
+            self.next_slot = (slot + 1) % self.depth
+            stream = self.slot_streams[slot]
+            ready = torch.cuda.Event()
+            ready.record(torch.cuda.current_stream(self.device))
+            stream.wait_event(ready)
+            with torch.cuda.stream(stream):
+                if self.slot_info[slot].numel() != batch:
+                    self.slot_info[slot] = torch.zeros(batch, dtype=torch.int32, device=self.device)
+                    self.slot_info[slot].record_stream(stream)
+                return self._run_mirror(hA, hB, hL, hX, hinfo, slot)
         if self.info.numel() != batch:
             self.info = torch.zeros(batch, dtype=torch.int32, device=self.device)
         if self.transport == "mirror":
-            return self._run_mirror(hA, hB, hL, hX, hinfo)
+            self.slot_info[0] = self.info
+            return self._run_mirror(hA, hB, hL, hX, hinfo, 0)
         if self.transport == "direct":
             return self._run_direct(hA, hB, hL, hX, hinfo)
         cur = torch.cuda.current_stream(self.device)
@@ -134,20 +163,31 @@ class PosvHostPipeline:
         cur.wait_event(fin)
         return self.info
 
-    def _run_mirror(self, hA, hB, hL, hX, hinfo):
+    def wait(self):
+        """Makes the current stream wait for every batch in flight (depth > 1; nothing to do
+        otherwise, since run() then enqueues on the current stream itself)."""
+        cur = torch.cuda.current_stream(self.device)
+        for s in getattr(self, "slot_streams", []):
+            done = torch.cuda.Event()
+            done.record(s)
+            cur.wait_event(done)
+
+    def _run_mirror(self, hA, hB, hL, hX, hinfo, slot):
         n, r = self.n, self.nrhs
         _check_host(n, r, hA, hB, hL, hX)
         batch = hA.shape[0]
         stream = torch.cuda.current_stream(self.device)
+        wL, wX = self.work[slot]
+        info = self.slot_info[slot]
         for b0 in range(0, batch, self.chunk):
             k = min(batch, b0 + self.chunk) - b0
             _lib.call("blastgpu_dposv_mirror_strided", n, r, hA[b0].data_ptr(), n, n * n,
                       hB[b0].data_ptr() if r else 0, n, n * r, hL[b0].data_ptr(), n, n * n,
-                      hX[b0].data_ptr() if r else 0, n, n * r, self.wL.data_ptr(), self.wX.data_ptr(),
-                      self.info[b0:].data_ptr(), k, stream.cuda_stream)
+                      hX[b0].data_ptr() if r else 0, n, n * r, wL.data_ptr(), wX.data_ptr(),
+                      info[b0:].data_ptr(), k, stream.cuda_stream)
         if hinfo is not None:
-            hinfo.copy_(self.info, non_blocking=True)
-        return self.info
+            hinfo.copy_(info, non_blocking=True)
+        return info
 
 
 def pinned_col_major(batch: int, rows: int, cols: int) -> torch.Tensor:

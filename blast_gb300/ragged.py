@@ -162,17 +162,9 @@ def capture_graph(fn):
 
 
 class GesvPlan:
-    """Ragged batch of LU solves (getrf + getrs), column-major A_i (n_i x n_i), B_i (n_i x r_i).
+    """Ragged batch of LU solves (getrf + getrs), column-major A_i (n_i x n_i), B_i (n_i x r_i)."""
 
-    The instances, sorted largest first, are cut into parts: the matrices with n <= 64 (one warp
-    per matrix) and `parts` slices of equal count of the larger ones (one CTA per matrix). Each
-    part's getrf and then its getrs run on a stream of their own, so that the solves of the largest
-    instances (thread per matrix, whose backward substitution is a serial chain in BLAST's order)
-    run while the smaller instances are still being factored. parts = 0 is the schedule without
-    overlap: the two getrf bins on forked streams, then one getrs launch over the whole batch.
-    Either way every instance sees the same operations, so the results are the same bits."""
-
-    def __init__(self, A: Packed, B: Packed, parts: int = 4):
+    def __init__(self, A: Packed, B: Packed):
         n = A.rows
         if np.any(A.cols != n) or np.any(B.rows != n):
             raise ValueError("Invalid argument size")
@@ -186,45 +178,24 @@ class GesvPlan:
         self.d = desc.upload(recs, device)
         self.info = torch.zeros(self.count, dtype=torch.int32, device=device)
         self._keep = (A, B)
+        # Two size bins for the factorisation (one CTA per matrix above n = 64, one warp per
+        # matrix below), on forked streams; the solves run as one launch afterwards.
         sorted_n = n[self.order]
         big = int(np.sum(sorted_n > 64))
-        self.overlap = parts > 0
         self.bins = [(b0, b1, int(sorted_n[b0])) for b0, b1 in ((0, big), (big, self.count)) if b1 > b0]
-        if self.overlap:
-            cuts = [0] + [big * k // parts for k in range(1, parts)] + [big]
-            spans = [(b0, b1) for b0, b1 in zip(cuts[:-1], cuts[1:]) if b1 > b0]
-            if self.count > big:
-                spans.append((big, self.count))
-            self.parts = [(b0, b1, int(sorted_n[b0])) for b0, b1 in spans]
-            self.streams = [torch.cuda.Stream(device) for _ in self.parts]
-        else:
-            self.side = torch.cuda.Stream(device)
+        self.side = torch.cuda.Stream(device)
 
     def _getrf(self, b0, b1, max_n, s):
         _lib.call("blastgpu_dgetrf_batched", self.d.data_ptr() + b0 * desc.GETRF_DTYPE.itemsize,
-                  self.info.data_ptr() + 4 * b0, b1 - b0, max_n, s)
-
-    def _getrs(self, b0, b1, max_n, s):
-        _lib.call("blastgpu_dgetrs_batched", self.d.data_ptr() + b0 * desc.GETRF_DTYPE.itemsize,
                   self.info.data_ptr() + 4 * b0, b1 - b0, max_n, s)
 
     def run(self, stream=None):
         cur = stream or torch.cuda.current_stream()
         if not self.bins:
             return
-        start = torch.cuda.Event()
-        start.record(cur)
-        if self.overlap:
-            for (b0, b1, mx), s in zip(self.parts, self.streams):
-                s.wait_event(start)
-                self._getrf(b0, b1, mx, s.cuda_stream)
-                self._getrs(b0, b1, mx, s.cuda_stream)
-            for s in self.streams:
-                done = torch.cuda.Event()
-                done.record(s)
-                cur.wait_event(done)
-            return
         if len(self.bins) == 2:
+            start = torch.cuda.Event()
+            start.record(cur)
             self.side.wait_event(start)
             self._getrf(*self.bins[1], self.side.cuda_stream)
         self._getrf(*self.bins[0], cur.cuda_stream)
@@ -232,7 +203,8 @@ class GesvPlan:
             done = torch.cuda.Event()
             done.record(self.side)
             cur.wait_event(done)
-        self._getrs(0, self.count, self.bins[0][2], cur.cuda_stream)
+        _lib.call("blastgpu_dgetrs_batched", self.d.data_ptr(), self.info.data_ptr(), self.count,
+                  self.bins[0][2], cur.cuda_stream)
 
     def capture(self):
         """Records run() into a CUDA graph; returns the torch.cuda.CUDAGraph (call .replay())."""

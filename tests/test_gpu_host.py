@@ -1,7 +1,8 @@
 """Host-resident batches (blast_gb300.host.PosvHostPipeline): the three transports — staged copies over
 three streams; the kernel reading A, B from pinned host memory with staged result copies; and the
 kernel that also writes L, X to host memory (blastgpu_dposv_mirror_strided) — give the
-device-resident posv's results bit for bit."""
+device-resident posv's results bit for bit, and so does the mirror transport with several batches
+in flight."""
 import numpy as np
 import pytest
 
@@ -49,6 +50,41 @@ def test_host_pipeline_matches_device_posv(gpu, transport, n, nrhs, batch, chunk
     assert torch.equal(torch.tril(hL), torch.tril(dL.cpu()))
     if nrhs:
         assert torch.equal(hX, dX.cpu())
+
+
+@pytest.mark.parametrize("depth,steps", [(2, 5), (3, 7)])
+def test_mirror_pipeline_batches_in_flight(gpu, depth, steps):
+    """With depth > 1 consecutive run() calls overlap on the pipeline's own streams, each with its
+    own device workspace; every batch (different inputs per call, output buffers per slot) still
+    gives the device-resident posv's bits once wait() has joined them."""
+    import torch
+
+    from blast_gb300.host import PosvHostPipeline, pinned_col_major
+
+    n, nrhs, batch = 48, 8, 6000
+    rng = np.random.default_rng(depth * 100 + steps)
+    inputs = [_inputs(rng, batch, n, nrhs) for _ in range(steps)]
+    outs = [(pinned_col_major(batch, n, n), pinned_col_major(batch, n, nrhs),
+             torch.full((batch,), -5, dtype=torch.int32).pin_memory()) for _ in range(steps)]
+    for hL, hX, _ in outs:
+        hL.zero_()
+        hX.zero_()
+    pipe = PosvHostPipeline(n, nrhs, batch, "cuda", transport="mirror", depth=depth)
+    for (hA, hB), (hL, hX, hinfo) in zip(inputs, outs):
+        pipe.run(hA, hB, hL, hX, hinfo)
+    pipe.wait()
+    torch.cuda.synchronize()
+    for (hA, hB), (hL, hX, hinfo) in zip(inputs, outs):
+        dA, dB = hA.cuda(), hB.cuda()
+        dL, dX = gpu.col_major((batch,), n, n, "cuda"), gpu.col_major((batch,), n, nrhs, "cuda")
+        dL.zero_()
+        info = gpu.posv(dA, dL, dB, dX)
+        torch.cuda.synchronize()
+        assert not hinfo.any() and not info.any()
+        assert torch.equal(torch.tril(hL), torch.tril(dL.cpu()))
+        assert torch.equal(hX, dX.cpu())
+    with pytest.raises(ValueError):
+        PosvHostPipeline(n, nrhs, batch, "cuda", transport="copy", depth=2)
 
 
 def test_zero_copy_rejects_pageable_buffers(gpu):

@@ -97,7 +97,9 @@ def test_ragged_posv_mixed_factorisations(gpu, mode):
     3xTF32 update, 2: tensor-core update with binary64 diagonal blocks, 3: CUDA-core update with
     binary64 diagonal blocks) over every size bin (n <= 64, 128, 256, 512, including sizes that are
     not multiples of 16 or 32) converges to the backward-error tolerance and agrees with the
-    binary64 path."""
+    binary64 path. A mode other than 0 must also give other bits than mode 0 on some instance,
+    which shows that the selected factorisation ran (the per-bin keys of the tuning cache take
+    precedence over the global one, so all of them are set)."""
     import torch
 
     from blast_gb300 import _lib
@@ -113,14 +115,23 @@ def test_ragged_posv_mixed_factorisations(gpu, mode):
     B = Packed(ns, [1] * len(ns), "cuda")
     B.fill_from(Bs)
     X, X64, L64 = Packed(ns, [1] * len(ns), "cuda"), Packed(ns, [1] * len(ns), "cuda"), Packed(ns, ns, "cuda")
-    old = _lib.tune_get("posv.mixed")
-    _lib.tune_set("posv.mixed", mode)
+    keys = ["posv.mixed"] + [f"posv.mixed.n{b}" for b in (8, 16, 32, 64, 128, 256, 512)]
+    old = {k: _lib.tune_get(k) for k in keys}
+    X0 = Packed(ns, [1] * len(ns), "cuda")
     try:
+        for k in keys:
+            _lib.tune_set(k, 0)
+        PosvPlan(A, B, X0, mixed=True, tol=1e-12, max_iter=20).run()
+        for k in keys:
+            _lib.tune_set(k, mode)
         plan = PosvPlan(A, B, X, mixed=True, tol=1e-12, max_iter=20)
         plan.run()
         torch.cuda.synchronize()
     finally:
-        _lib.tune_set("posv.mixed", old if old is not None else 0)
+        for k, v in old.items():
+            _lib.tune_set(k, v if v is not None else 0)
+    if mode != 0:
+        assert any(not np.array_equal(a, b) for a, b in zip(X.to_list(), X0.to_list()))
     PosvPlan(A, B, X64, L64).run()
     torch.cuda.synchronize()
     info, iters, berr = plan.results()
