@@ -16,9 +16,11 @@
 //    column, scaling and rank-1 updates lane per row, the trailing update lane per element.
 //    Every element sees exactly BLAST's sequence of rounded operations (the pivot scaling is an
 //    IEEE division, as in BLAST), so factors and pivot sequences are bit-identical to the oracle.
-//  * getrs: one thread per matrix. The backward substitution is a chain of dependent dot
-//    products in BLAST's order (each x_i starts from x_{i+1}); running whole solves per thread
-//    keeps every lane busy while preserving that order.
+//  * getrs: the forward half (laswp(b), unit-lower solve) one warp per matrix for n <= 256, lanes
+//    over rows in a column sweep that keeps every row's ascending order; the backward half one
+//    thread per matrix. The backward substitution is a chain of dependent dot products in BLAST's
+//    order (each x_i starts from x_{i+1}); running it per thread keeps every lane busy while
+//    preserving that order.
 #include <atomic>
 
 #include "common.cuh"
@@ -534,8 +536,102 @@ __device__ __forceinline__ void load_pass(FactorView const& A, int i, int k0, in
     for (int u = 0; u < 16; ++u) av[u] = k0 + u < k1 ? A(i, k0 + u) : 0.0;
 }
 
+// The forward half of getrs with one warp per instance, for n <= 32 * MAXT: the row interchanges
+// of b in ipiv order (lane 0, in shared memory), then y_i = b_i - sum_{l<i} l_il y_l as a column
+// sweep with lanes over rows: once y_l is final its owner lane broadcasts it and every row below
+// takes its term. Each row's sum still runs in ascending l with the same fused multiply-adds as the
+// thread kernel's (and BLAST's) order, so y is the same bits; the rows advance together, and the
+// factor's columns are read coalesced, four columns ahead of their use. y overwrites b; the
+// backward half then runs one thread per instance (getrs_kernel with fwd = 0), whose chain is
+// serial in BLAST's order.
+// One pass of the backward substitution: row i, terms k0 .. k0+15 (row i's first pass starts at
+// k0 = i + 1 and also loads the diagonal u_ii). Passes run bottom row first; i < 0 ends the
+// sequence.
+struct BwdPass {
+    int i, k0;
+    __device__ __forceinline__ BwdPass next(int n) const {
+        if (i < 0) return *this;
+        return k0 + 16 < n ? BwdPass{i, k0 + 16} : BwdPass{i - 1, i};
+    }
+    __device__ __forceinline__ void load(FactorView const& A, int n, double (&av)[16], double& d) const {
+        load_pass(A, i, k0, n, av);
+        if (k0 == i + 1) d = A(i, i);
+    }
+};
+
+template <int MAXT>
+struct FwdCols {
+    double v[4][MAXT];
+    __device__ __forceinline__ void load(FactorView const& A, int s, int l, int n, int lane) {
+#pragma unroll
+        for (int t = 0; t < MAXT; ++t) {
+            int const i = lane + 32 * t;
+            v[s][t] = (l < n && i > l && i < n) ? A(i, l) : 0.0;
+        }
+    }
+};
+
+template <int MAXT, class Batch>
+__global__ void __launch_bounds__(kWarps * 32) getrs_fwd_warp_kernel(Batch batch, int64_t count, const int32_t* info) {
+    __shared__ double ys[kWarps][32 * MAXT];
+    int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int64_t const b = (int64_t)blockIdx.x * kWarps + warp;
+    if (b >= count) return;
+    if (info && info[b] != 0) return;
+    GetrsItem const it = batch.get(b);
+    int const n = it.n;
+    FactorView const A{it.a, it.lda};
+    double* y = ys[warp];
+    for (int j = 0; j < it.nrhs; ++j) {
+        double* bj = it.x + (int64_t)j * it.ldx;
+        __syncwarp();
+        for (int k = lane; k < n; k += 32) y[k] = bj[k];
+        __syncwarp();
+        if (lane == 0) {
+            for (int k = 0; k < n; ++k) {
+                int const q = it.ipiv[k];
+                if (q != k) {
+                    double const t = y[k];
+                    y[k] = y[q];
+                    y[q] = t;
+                }
+            }
+        }
+        __syncwarp();
+        double acc[MAXT];
+#pragma unroll
+        for (int t = 0; t < MAXT; ++t) acc[t] = lane + 32 * t < n ? y[lane + 32 * t] : 0.0;
+        FwdCols<MAXT> c;
+#pragma unroll
+        for (int s = 0; s < 4; ++s) c.load(A, s, s, n, lane);
+        for (int l0 = 0; l0 < n - 1; l0 += 4) {
+#pragma unroll
+            for (int s = 0; s < 4; ++s) {
+                int const l = l0 + s;
+                if (l < n - 1) {
+                    int const tl = l >> 5;
+                    double own = 0.0;
+#pragma unroll
+                    for (int t = 0; t < MAXT; ++t)
+                        if (t == tl) own = acc[t];
+                    double const yl = __shfl_sync(0xffffffffu, own, l & 31);
+#pragma unroll
+                    for (int t = 0; t < MAXT; ++t) {
+                        int const i = lane + 32 * t;
+                        if (t >= tl && i > l && i < n) acc[t] = fma(-c.v[s][t], yl, acc[t]);
+                    }
+                }
+                c.load(A, s, l + 4, n, lane);
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < MAXT; ++t)
+            if (lane + 32 * t < n) bj[lane + 32 * t] = acc[t];
+    }
+}
+
 template <class Batch>
-__global__ void __launch_bounds__(32) getrs_kernel(Batch batch, int64_t count, const int32_t* info) {
+__global__ void __launch_bounds__(32) getrs_kernel(Batch batch, int64_t count, const int32_t* info, int fwd) {
     extern __shared__ double xs[];
     int const lane = threadIdx.x;
     int64_t const b = (int64_t)blockIdx.x * 32 + lane;
@@ -548,7 +644,7 @@ __global__ void __launch_bounds__(32) getrs_kernel(Batch batch, int64_t count, c
     for (int j = 0; j < it.nrhs; ++j) {
         const double* bj = it.x + (int64_t)j * it.ldx;
         for (int k = 0; k < n; ++k) x[k * 32] = bj[k];
-        for (int k = 0; k < n; ++k) {
+        for (int k = 0; k < n && fwd; ++k) {
             int const q = it.ipiv[k];
             if (q != k) {
                 double const t = x[k * 32];
@@ -556,7 +652,7 @@ __global__ void __launch_bounds__(32) getrs_kernel(Batch batch, int64_t count, c
                 x[q * 32] = t;
             }
         }
-        for (int i0 = 0; i0 < n; i0 += 4) {
+        for (int i0 = 0; i0 < n && fwd; i0 += 4) {
             double acc[4];
 #pragma unroll
             for (int r = 0; r < 4; ++r) acc[r] = i0 + r < n ? x[(i0 + r) * 32] : 0.0;
@@ -595,30 +691,46 @@ __global__ void __launch_bounds__(32) getrs_kernel(Batch batch, int64_t count, c
             }
         }
         {
-            int i = n - 1, k0 = n;
-            double av[16], acc = 0.0;
-            load_pass(A, i, k0, n, av);
-            double d = A(i, i);
-            while (i >= 0) {
-                int ni = i, nk = k0 + 16;
-                if (nk >= n) { ni = i - 1; nk = i; }
-                double an[16], dn = 0.0;
-                if (ni >= 0) {
-                    load_pass(A, ni, nk, n, an);
-                    if (ni != i) dn = A(ni, ni);
-                }
-                if (k0 == i + 1) acc = x[i * 32];
+            // Passes of 16 terms along each row, bottom row first, with kSlots passes in flight:
+            // the loop is unrolled over kSlots register slots, and a slot is reloaded with the pass
+            // kSlots ahead right after its FMAs, so no load result is ever copied (a copy would
+            // wait for it) and each load has kSlots - 1 passes of FMAs to arrive.
+            constexpr int kSlots = 3;
+            BwdPass p[kSlots];
+            double a[kSlots][16], dg[kSlots];
+            p[0] = BwdPass{n - 1, n};
 #pragma unroll
-                for (int u = 0; u < 16; ++u)
-                    if (k0 + u < n) acc = fma(-av[u], x[(k0 + u) * 32], acc);
-                if (ni != i) {
-                    x[i * 32] = acc / d;
-                    d = dn;
-                }
-                i = ni;
-                k0 = nk;
+            for (int s = 1; s < kSlots; ++s) p[s] = p[s - 1].next(n);
 #pragma unroll
-                for (int u = 0; u < 16; ++u) av[u] = an[u];
+            for (int s = 0; s < kSlots; ++s) {
+                dg[s] = 0.0;
+                if (p[s].i >= 0) p[s].load(A, n, a[s], dg[s]);
+            }
+            BwdPass nxt = p[kSlots - 1].next(n);
+            double acc = 0.0, drow = 0.0;
+            bool done = false;
+            while (!done) {
+#pragma unroll
+                for (int s = 0; s < kSlots; ++s) {
+                    if (!done) {
+                        BwdPass const cur = p[s];
+                        if (cur.i < 0) {
+                            done = true;
+                        } else {
+                            if (cur.k0 == cur.i + 1) {
+                                acc = x[cur.i * 32];
+                                drow = dg[s];
+                            }
+#pragma unroll
+                            for (int u = 0; u < 16; ++u)
+                                if (cur.k0 + u < n) acc = fma(-a[s][u], x[(cur.k0 + u) * 32], acc);
+                            if (p[(s + 1) % kSlots].i != cur.i) x[cur.i * 32] = acc / drow;
+                            p[s] = nxt;
+                            if (nxt.i >= 0) nxt.load(A, n, a[s], dg[s]);
+                            nxt = nxt.next(n);
+                        }
+                    }
+                }
             }
         }
         double* out = it.x + (int64_t)j * it.ldx;
@@ -667,7 +779,23 @@ int launch_getrs(Batch const& batch, int64_t count, int max_n, const int32_t* in
         cudaError_t const e = ensure_smem<getrs_kernel<Batch>>(200 * 1024);
         if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
     }
-    getrs_kernel<Batch><<<(unsigned)blocks, 32, smem, s>>>(batch, count, info);
+    // "getrs.warp_fwd" (default 1): the forward half one warp per instance for n <= 256, then
+    // the backward half one thread per instance; 0: both halves one thread per instance.
+    int const maxt = (max_n + 31) / 32;
+    if (max_n <= 256 && tune_get("getrs.warp_fwd", 1) != 0) {
+        int64_t const wblocks = (count + kWarps - 1) / kWarps;
+        if (wblocks > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
+        switch (maxt) {
+            case 1: getrs_fwd_warp_kernel<1, Batch><<<(unsigned)wblocks, kWarps * 32, 0, s>>>(batch, count, info); break;
+            case 2: getrs_fwd_warp_kernel<2, Batch><<<(unsigned)wblocks, kWarps * 32, 0, s>>>(batch, count, info); break;
+            case 3:
+            case 4: getrs_fwd_warp_kernel<4, Batch><<<(unsigned)wblocks, kWarps * 32, 0, s>>>(batch, count, info); break;
+            default: getrs_fwd_warp_kernel<8, Batch><<<(unsigned)wblocks, kWarps * 32, 0, s>>>(batch, count, info); break;
+        }
+        getrs_kernel<Batch><<<(unsigned)blocks, 32, smem, s>>>(batch, count, info, 0);
+    } else {
+        getrs_kernel<Batch><<<(unsigned)blocks, 32, smem, s>>>(batch, count, info, 1);
+    }
     return check_launch();
 }
 

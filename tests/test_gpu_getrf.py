@@ -219,22 +219,28 @@ def test_getrs_large_n_bitexact(gpu, oracle_lib, n):
         assert np.array_equal(X[b], Xr), n
 
 
-def test_getrf_kernel_choice_keeps_bits(gpu, oracle_lib):
+@pytest.mark.parametrize("ns", [[7, 40, 65, 100, 129, 200, 256, 31, 1, 4, 5, 8, 9, 33, 67, 97, 130, 255, 300, 512],
+                                [7, 40, 65, 100, 129, 200, 256, 31, 1, 4, 5, 8, 9, 33, 67, 97, 130, 255, 2, 3],
+                                [3, 17, 33, 64, 1, 100, 97, 128, 31, 32],
+                                [1, 2, 3, 5, 8, 13, 21, 32, 30]])
+def test_getrf_kernel_choice_keeps_bits(gpu, oracle_lib, ns):
     """The autotuner's per-bin choices between the warp-per-matrix LU kernel, the CTA kernel's
-    right-looking schedule and its left-looking schedule ("getrf.cta.n<bin>", "getrf.lazy.n<bin>")
-    change the schedule, never the result: factors, pivots and solutions are identical under every
-    choice and equal to the oracle's."""
+    right-looking schedule and its left-looking schedule ("getrf.cta.n<bin>", "getrf.lazy.n<bin>"),
+    and getrs with its forward half one warp per instance or one thread per instance
+    ("getrs.warp_fwd"; the warp form serves batches with n <= 256, so the largest n of each case
+    selects its register tile) change the schedule, never the result: factors, pivots and
+    solutions are identical under every choice and equal to the oracle's."""
     import torch
 
     from blast_gb300 import _lib
     from blast_gb300.ragged import GesvPlan, Packed
 
     rng = np.random.default_rng(91)
-    ns = [7, 40, 65, 100, 129, 200, 256, 31, 1, 4, 5, 8, 9, 33, 67, 97, 130, 255, 300, 512]
     mats = [rng.standard_normal((n, n)) for n in ns]
     bins = (8, 16, 32, 64, 128, 256, 512)
     results = []
-    for cta, lazy in ((0, 0), (1, 0), (1, 1)):
+    for cta, lazy, warp_fwd in ((0, 0, 1), (1, 0, 1), (1, 1, 1), (1, 0, 0)):
+        _lib.tune_set("getrs.warp_fwd", warp_fwd)
         for b in bins:
             _lib.tune_set(f"getrf.cta.n{b}", cta)
             _lib.tune_set(f"getrf.lazy.n{b}", lazy)
@@ -248,6 +254,7 @@ def test_getrf_kernel_choice_keeps_bits(gpu, oracle_lib):
             torch.cuda.synchronize()
             results.append((A.to_list(), plan.pivots(), B.to_list(), plan.info_host()))
         finally:
+            _lib.tune_set("getrs.warp_fwd", 1)
             for b in bins:
                 _lib.tune_set(f"getrf.cta.n{b}", 1 if b > 64 else 0)
                 _lib.tune_set(f"getrf.lazy.n{b}", 0)
