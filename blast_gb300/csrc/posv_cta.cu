@@ -1236,6 +1236,9 @@ int blastgpu_dposv_batched(const blastgpu_posv_desc* desc, int64_t batch, int ma
     if (!desc) return -1;
     if (max_n < 0) return -3;
     if (max_n > 512) return BLASTGPU_ERR_TOO_LARGE;
+    // "posv.warp.n<bin>" (default 1): batches with every n <= 128 on the warp-per-matrix kernel
+    if (max_n <= 128 && tune_get_bin("posv.warp", max_n, 1) != 0)
+        return launch_posv_warp(desc, batch, max_n, info, as_cuda(stream));
     CtaArgs a{batch, info, nullptr, nullptr, 0.0, 0};
     return dispatch_cta(false, max_n, DescPosv{desc, nullptr}, a, as_cuda(stream));
 }

@@ -1,4 +1,5 @@
-"""Ragged Cholesky solves (one CTA per matrix): the binary64 path against the oracle and the
+"""Ragged Cholesky solves (one CTA per matrix; one warp per matrix for small n): the binary64 path
+against the oracle and the
 mixed-precision path (binary32 factor + binary64 refinement) against the 1e-12 backward-error bar.
 """
 import numpy as np
@@ -53,6 +54,74 @@ def test_ragged_posv_fp64_matches_oracle(gpu, oracle_lib):
         oracle_lib.potrs(Lr, np.asfortranarray(Bh), Xr)
         assert normwise(np.tril(Lg), Lr) <= 10 * n * EPS, n
         assert normwise(Xg, Xr) <= 100 * n * EPS, n
+
+
+@pytest.mark.parametrize("ns", [[1, 2, 3, 4, 5, 7, 8, 9, 16, 17, 31, 32],
+                                [33, 40, 63, 64, 1, 12, 48, 57],
+                                [65, 100, 127, 128, 1, 4, 31, 64, 97, 120, 66, 5]])
+def test_ragged_posv_small_warp_kernel(gpu, ns):
+    """Ragged binary64 batches with every n <= 128 run one warp per matrix ("posv.warp.n<bin>").
+    Its fused multiply-adds are the thread-per-matrix kernel's, in the same order, so L and X are
+    the same bits as the uniform thread kernel's on each instance. They also agree with the CTA
+    kernel, the other choice for the same bins, within 10 n eps, and a non-positive-definite
+    instance reports the same info as the thread kernel."""
+    import torch
+
+    from blast_gb300 import _lib
+    from blast_gb300.ragged import Packed, PosvPlan
+
+    rng = np.random.default_rng(sum(ns))
+    nrhs = [1 + (i % 3) for i in range(len(ns))]
+    As = [G @ G.T + n * np.eye(n) for G, n in ((rng.standard_normal((n, n)), n) for n in ns)]
+    bad = len(ns) // 2
+    if ns[bad] > 2:
+        As[bad] = As[bad].copy()
+        As[bad][2, 2] = -1.0  # not positive definite: the third pivot fails
+    Bs = [rng.standard_normal((n, r)) for n, r in zip(ns, nrhs)]
+
+    def solve(warp):
+        A = Packed(ns, ns, "cuda")
+        A.fill_from(As)
+        B = Packed(ns, nrhs, "cuda")
+        B.fill_from(Bs)
+        X, L = Packed(ns, nrhs, "cuda"), Packed(ns, ns, "cuda")
+        keys = [f"posv.warp.n{b}" for b in (8, 16, 32, 64, 128)]
+        old = {k: _lib.tune_get(k) for k in keys}
+        try:
+            for k in keys:
+                _lib.tune_set(k, warp)
+            plan = PosvPlan(A, B, X, L)
+            plan.run()
+            torch.cuda.synchronize()
+        finally:
+            for k, v in old.items():
+                _lib.tune_set(k, v if v is not None else 1)
+        return [np.tril(m) for m in L.to_list()], X.to_list(), plan.results()[0]
+
+    Lw, Xw, infow = solve(1)
+    Lc, Xc, infoc = solve(0)
+    old_min = _lib.tune_get("posv.cta_min_n")
+    _lib.tune_set("posv.cta_min_n", 513)  # uniform batches on the thread-per-matrix kernel
+    try:
+        for i, (n, Ah, Bh) in enumerate(zip(ns, As, Bs)):
+            dA = gpu.col_major((1,), n, n, "cuda")
+            dA.copy_(torch.from_numpy(Ah[None]))
+            dB = gpu.col_major((1,), n, nrhs[i], "cuda")
+            dB.copy_(torch.from_numpy(Bh[None]))
+            dL, dX = gpu.col_major((1,), n, n, "cuda"), gpu.col_major((1,), n, nrhs[i], "cuda")
+            dL.zero_()
+            info_t = gpu.posv(dA, dL, dB, dX)
+            torch.cuda.synchronize()
+            assert int(info_t[0]) == int(infow[i]) == int(infoc[i]), (n, int(info_t[0]), int(infow[i]), int(infoc[i]))
+            if infow[i] != 0:
+                continue
+            assert np.array_equal(Lw[i], np.tril(dL.cpu().numpy()[0])), n
+            assert np.array_equal(Xw[i], dX.cpu().numpy()[0]), n
+            assert normwise(Lw[i], Lc[i]) <= 10 * n * EPS, n
+            assert normwise(Xw[i], Xc[i]) <= 100 * n * EPS, n
+    finally:
+        _lib.tune_set("posv.cta_min_n", old_min if old_min is not None else 129)
+    assert ns[bad] <= 2 or infow[bad] == 3
 
 
 @pytest.mark.parametrize("cond", [1e2, 1e4, 1e6])
