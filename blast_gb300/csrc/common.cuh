@@ -64,6 +64,9 @@ int launch_posv_cta_strided(int n, int nrhs, const double* A, int lda, int64_t s
 // Ragged binary64 Cholesky solves with every n <= 128 on the warp-per-matrix kernel of
 // posv_warp.cu (descriptors as for blastgpu_dposv_batched).
 int launch_posv_warp(const blastgpu_posv_desc* desc, int64_t count, int max_n, int32_t* info, cudaStream_t s);
+// Their adjoints (descriptors as for blastgpu_dposv_bwd_batched), one warp per matrix.
+int launch_posv_bwd_warp(const blastgpu_posv_bwd_desc* desc, int64_t count, int max_n, int recompute, int32_t* info,
+                         cudaStream_t s);
 
 // Kernel-selection parameters set by the autotuner (blastgpu_tune_set); `fallback` if unset.
 int tune_get(const char* key, int fallback);

@@ -1268,6 +1268,9 @@ int blastgpu_dposv_bwd_batched(const blastgpu_posv_bwd_desc* desc, int64_t batch
     if (batch > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
     DescBwd d{desc};
     cudaStream_t const s = as_cuda(stream);
+    // "posv.warp_bwd.n<bin>" (default 1): batches with every n <= 128 one warp per matrix
+    if (max_n <= 128 && tune_get_bin("posv.warp_bwd", max_n, 1) != 0)
+        return launch_posv_bwd_warp(desc, batch, max_n, recompute, info, s);
     if (max_n <= 64) return launch_bwd<2>(d, batch, recompute, info, s);
     if (max_n <= 128) return launch_bwd<4>(d, batch, recompute, info, s);
     if (max_n <= 256) return launch_bwd<8>(d, batch, recompute, info, s);

@@ -219,6 +219,19 @@ __device__ void warp_potrs_column(int n, const double* L, int ldl, const double*
     __syncwarp();
 }
 
+// One instance with n <= 32 NB: its row blocks (NB of them) fix the register tiles, so the
+// blocks past its last row cost nothing.
+template <int NB>
+__device__ __forceinline__ void warp_posv(blastgpu_posv_desc const& dsc, int n, double* xs, int lane, int32_t* info_b) {
+    if (dsc.A.data != nullptr) {  // A == nullptr: solves with the given factor L only
+        int const r = warp_potrf<NB>(n, dsc.A.data, dsc.A.ld, dsc.L.data, dsc.L.ld, lane);
+        if (info_b && lane == 0) *info_b = r;
+    }
+    for (int j = 0; j < dsc.B.cols; ++j)
+        warp_potrs_column<NB>(n, dsc.L.data, dsc.L.ld, dsc.B.data + (int64_t)j * dsc.B.ld,
+                              dsc.X.data + (int64_t)j * dsc.X.ld, xs, lane);
+}
+
 template <int MAXT>
 __global__ void __launch_bounds__(kWarpsPerCta * 32) posv_warp_kernel(const blastgpu_posv_desc* desc, int64_t count,
                                                                      int32_t* info) {
@@ -229,16 +242,99 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) posv_warp_kernel(const blas
     blastgpu_posv_desc const& dsc = desc[b];
     int const n = dsc.A.rows;
     if (n > 32 * MAXT) return;  // the launch's max_n bounds every instance
-    if (dsc.A.data != nullptr) {  // A == nullptr: solves with the given factor L only
-        int const r = warp_potrf<MAXT>(n, dsc.A.data, dsc.A.ld, dsc.L.data, dsc.L.ld, lane);
-        if (info && lane == 0) info[b] = r;
+    int32_t* const info_b = info ? info + b : nullptr;
+    switch ((n + 31) >> 5) {
+        case 0:
+        case 1: warp_posv<1>(dsc, n, xs_all[w], lane, info_b); break;
+        case 2: if constexpr (MAXT >= 2) warp_posv<(MAXT >= 2 ? 2 : 1)>(dsc, n, xs_all[w], lane, info_b); break;
+        case 3: if constexpr (MAXT >= 3) warp_posv<(MAXT >= 3 ? 3 : 1)>(dsc, n, xs_all[w], lane, info_b); break;
+        default: if constexpr (MAXT >= 4) warp_posv<(MAXT >= 4 ? 4 : 1)>(dsc, n, xs_all[w], lane, info_b); break;
     }
-    for (int j = 0; j < dsc.B.cols; ++j)
-        warp_potrs_column<MAXT>(n, dsc.L.data, dsc.L.ld, dsc.B.data + (int64_t)j * dsc.B.ld,
-                                dsc.X.data + (int64_t)j * dsc.X.ld, xs_all[w], lane);
+}
+
+// Adjoint of X = A^{-1} B for one instance, one warp (as posv_bwd_kernel, which runs a CTA per
+// matrix): the factor kept in L or recomputed from A, dl/dB = A^{-1} dl/dX with the warp's solve,
+// dl/dA = -(dl/dB X^T + X dl/dB^T)/2 written by lanes over rows, a column at a time.
+template <int NB>
+__device__ __forceinline__ void warp_posv_bwd(blastgpu_posv_bwd_desc const& d, int n, int recompute, double* xs,
+                                              int lane, int32_t* info_b) {
+    if (recompute) {
+        int const r = warp_potrf<NB>(n, d.A.data, d.A.ld, d.L.data, d.L.ld, lane);
+        if (info_b && lane == 0) *info_b = r;
+    } else if (info_b && lane == 0) {
+        *info_b = 0;
+    }
+    int const nrhs = d.X.cols;
+    for (int c = 0; c < nrhs; ++c)
+        warp_potrs_column<NB>(n, d.L.data, d.L.ld, d.Xbar.data + (int64_t)c * d.Xbar.ld,
+                              d.Bbar.data + (int64_t)c * d.Bbar.ld, xs, lane);
+    if (nrhs == 1) {  // dl/dB is still in xs
+        double xi[NB], gi[NB];
+#pragma unroll
+        for (int t = 0; t < NB; ++t) {
+            int const i = lane + 32 * t;
+            xi[t] = i < n ? d.X.data[i] : 0.0;
+            gi[t] = i < n ? xs[i] : 0.0;
+        }
+        for (int j = 0; j < n; ++j) {
+            double const xj = d.X.data[j], gj = xs[j];
+            double* ga = d.Abar.data + (int64_t)j * d.Abar.ld;
+#pragma unroll
+            for (int t = 0; t < NB; ++t) {
+                int const i = lane + 32 * t;
+                if (i < n) ga[i] = -0.5 * fma(xi[t], gj, gi[t] * xj);
+            }
+        }
+        return;
+    }
+    __syncwarp();  // dl/dB columns are complete in memory
+    for (int j = 0; j < n; ++j)
+        for (int i = lane; i < n; i += 32) {
+            double acc = 0.0;
+            for (int c = 0; c < nrhs; ++c) {
+                acc = fma(d.Bbar.data[i + (int64_t)c * d.Bbar.ld], d.X.data[j + (int64_t)c * d.X.ld], acc);
+                acc = fma(d.X.data[i + (int64_t)c * d.X.ld], d.Bbar.data[j + (int64_t)c * d.Bbar.ld], acc);
+            }
+            d.Abar.data[i + (int64_t)j * d.Abar.ld] = -0.5 * acc;
+        }
+}
+
+template <int MAXT>
+__global__ void __launch_bounds__(kWarpsPerCta * 32) posv_bwd_warp_kernel(const blastgpu_posv_bwd_desc* desc,
+                                                                         int64_t count, int recompute, int32_t* info) {
+    __shared__ double xs_all[kWarpsPerCta][32 * MAXT];
+    int const w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int64_t const b = (int64_t)blockIdx.x * kWarpsPerCta + w;
+    if (b >= count) return;
+    blastgpu_posv_bwd_desc const& d = desc[b];
+    int const n = d.A.rows;
+    if (n > 32 * MAXT) return;  // the launch's max_n bounds every instance
+    int32_t* const info_b = info ? info + b : nullptr;
+    switch ((n + 31) >> 5) {
+        case 0:
+        case 1: warp_posv_bwd<1>(d, n, recompute, xs_all[w], lane, info_b); break;
+        case 2: if constexpr (MAXT >= 2) warp_posv_bwd<(MAXT >= 2 ? 2 : 1)>(d, n, recompute, xs_all[w], lane, info_b); break;
+        case 3: if constexpr (MAXT >= 3) warp_posv_bwd<(MAXT >= 3 ? 3 : 1)>(d, n, recompute, xs_all[w], lane, info_b); break;
+        default: if constexpr (MAXT >= 4) warp_posv_bwd<(MAXT >= 4 ? 4 : 1)>(d, n, recompute, xs_all[w], lane, info_b); break;
+    }
 }
 
 }  // namespace
+
+// Adjoints of ragged binary64 Cholesky solves with every n <= 128, one warp per matrix
+// (blastgpu_dposv_bwd_batched routes such launches here unless "posv.warp_bwd.n<bin>" is 0).
+int launch_posv_bwd_warp(const blastgpu_posv_bwd_desc* desc, int64_t count, int max_n, int recompute, int32_t* info,
+                         cudaStream_t s) {
+    if (count == 0) return BLASTGPU_SUCCESS;
+    int64_t const blocks = (count + kWarpsPerCta - 1) / kWarpsPerCta;
+    if (blocks > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
+    unsigned const g = (unsigned)blocks, t = kWarpsPerCta * 32;
+    if (max_n <= 32) posv_bwd_warp_kernel<1><<<g, t, 0, s>>>(desc, count, recompute, info);
+    else if (max_n <= 64) posv_bwd_warp_kernel<2><<<g, t, 0, s>>>(desc, count, recompute, info);
+    else if (max_n <= 128) posv_bwd_warp_kernel<4><<<g, t, 0, s>>>(desc, count, recompute, info);
+    else return BLASTGPU_ERR_TOO_LARGE;
+    return check_launch();
+}
 
 // Ragged binary64 Cholesky solves with every n <= 128, one warp per matrix (blastgpu_dposv_batched
 // routes such launches here unless "posv.warp.n<bin>" is 0).

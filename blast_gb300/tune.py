@@ -16,6 +16,8 @@ Tunable choices (read by the library through blastgpu_tune_set / tune_get_bin):
   if every instance converges.
 * ``posv.cta_min_n`` — uniform Cholesky batches from this n on run one CTA per matrix instead of one
   thread per matrix.
+* ``posv.warp.n<bin>`` — ragged binary64 Cholesky batches with every n <= 128: one warp (1) or one
+  CTA (0) per matrix (same bits as the thread kernel, or within 10 n eps of it).
 
 Results are cached as JSON keyed by GPU name (``blast_gb300/tuning/<gpu>.json``); ``apply()``
 loads the cache for the current GPU into the library, and ``import blast_gb300`` calls it.
@@ -230,6 +232,33 @@ def tune_posv_cta_min_n(ns=(48, 56, 64, 72, 80, 96, 112, 128), nrhs=8, batch=20_
     return {"posv.cta_min_n": int(value)}
 
 
+def tune_posv_warp(bins=(32, 64, 128), count: int = 4096) -> dict:
+    """Ragged binary64 Cholesky solves per size bin (n <= 128): one warp (1) or one CTA (0) per
+    matrix, on SPD matrices with n uniform in the bin and one right-hand side."""
+    import numpy as np
+
+    from .ragged import Packed, PosvPlan
+
+    rng = np.random.default_rng(6)
+    out = {}
+    for b in bins:
+        ns = rng.integers(max(1, b // 2 + 1), b + 1, count)
+        A = Packed(ns, ns, "cuda")
+        A.fill_from([G @ G.T + n * np.eye(n) for G, n in ((rng.standard_normal((n, n)), n) for n in ns)])
+        ones = np.ones_like(ns)
+        B, X, L = Packed(ns, ones, "cuda"), Packed(ns, ones, "cuda"), Packed(ns, ns, "cuda")
+        B.buf.normal_()
+        plan = PosvPlan(A, B, X, L)
+        key = f"posv.warp.n{size_bin(int(ns.max()))}"
+        times = {}
+        for v in (0, 1):
+            _lib.tune_set(key, v)
+            times[v] = _time(plan.run, reps=5)
+        out[key] = min(times, key=times.get)
+        _lib.tune_set(key, out[key])
+    return out
+
+
 def run(save: bool = True) -> dict:
     """Tunes every choice on the current GPU and (optionally) writes the cache."""
     choices = {}
@@ -238,6 +267,7 @@ def run(save: bool = True) -> dict:
     choices.update(tune_getrf())
     choices.update(tune_posv_mixed())
     choices.update(tune_posv_cta_min_n())
+    choices.update(tune_posv_warp())
     if save:
         CACHE_DIR.mkdir(parents=True, exist_ok=True)
         cache_path().write_text(json.dumps({"gpu": torch.cuda.get_device_name(),

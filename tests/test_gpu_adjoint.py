@@ -76,9 +76,29 @@ def test_spd_solve_finite_differences(gpu):
         assert abs(fd - np.sum(gb * W)) <= 1e-6 * max(1.0, abs(fd))
 
 
+@pytest.mark.parametrize("warp", [1, 0])
 @pytest.mark.parametrize("keep", [True, False])
-def test_spd_solve_packed_ragged_grad(gpu, keep):
-    """The differentiable workload's shape: ragged n in [32, 128], one right-hand side."""
+def test_spd_solve_packed_ragged_grad(gpu, keep, warp):
+    """The differentiable workload's shape: ragged n in [32, 128], one right-hand side, with the
+    forward solve and the adjoint one warp per matrix ("posv.warp.n<bin>", "posv.warp_bwd.n<bin>"
+    = 1) or one CTA per matrix (0)."""
+    import torch
+
+    from blast_gb300 import _lib
+    from blast_gb300.autograd import spd_solve_packed
+
+    keys = [f"posv.{p}.n{b}" for p in ("warp", "warp_bwd") for b in (8, 16, 32, 64, 128)]
+    old = {k: _lib.tune_get(k) for k in keys}
+    for k in keys:
+        _lib.tune_set(k, warp)
+    try:
+        _packed_ragged_grad(keep)
+    finally:
+        for k, v in old.items():
+            _lib.tune_set(k, v if v is not None else 1)
+
+
+def _packed_ragged_grad(keep):
     import torch
 
     from blast_gb300.autograd import spd_solve_packed
