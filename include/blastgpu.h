@@ -221,7 +221,8 @@ int blastgpu_dtrmm_strided(int side, int uplo, int unit, int m, int n, double al
 /* ---------------------------------------------------------------------------------------------
  * potrf: lower Cholesky factor L of a symmetric positive definite n x n A (only the lower
  * triangle of A is read; the strict upper triangle of L is not written). L may equal A. Uniform
- * batches with n >= 65 (tuning key posv.cta_min_n) run one CTA per matrix in panels of 32 columns
+ * batches with n >= posv.cta_min_n (a tuning key: 65 unless set; the GB300 tuning cache that the
+ * Python package applies sets 129) run one CTA per matrix in panels of 32 columns
  * (the ragged kernels' factorisation), below that one thread per matrix with BLAST's tiles; both
  * are within 10*n*eps of BLAST's algorithm. The same holds for posv and potrs below.
  * Replaces blast::potrf(A, L) dense (dense/Potrf.hpp:66-106) and panel (panel/Potrf.hpp:59-106).
