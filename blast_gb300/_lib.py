@@ -78,6 +78,8 @@ SIGNATURES: dict[str, list] = {
     "blastgpu_dgetrf_batched": [PTR, PTR, I64, I32, PTR],
     "blastgpu_dgetrs_batched": [PTR, PTR, I64, I32, PTR],
     "blastgpu_dgesv_batched": [PTR, PTR, I64, I32, PTR],
+    "blastgpu_dgesv_mixed_workspace_bytes": [I32],
+    "blastgpu_dgesv_mixed_batched": [PTR, I64, I32, PTR, DBL, I32, PTR, PTR, PTR, PTR],
     "blastgpu_dposv_mixed_workspace_bytes": [I32],
     "blastgpu_dsyrk_lower_strided": [I32, I32, DBL, PTR, I32, I64, DBL, PTR, I32, I64, PTR, I32, I64, I64, PTR],
     "blastgpu_dgemm_bwd_strided": [I32, I32, I32, I32, I32, DBL, PTR, I32, I64, PTR, I32, I64, DBL, PTR, I32, I64,
@@ -104,7 +106,8 @@ SIGNATURES: dict[str, list] = {
     "blastgpu_dpotrf_bwd_batched": [PTR, I64, PTR, PTR],
 }
 _RESTYPES = {"blastgpu_status_string": C.c_char_p, "blastgpu_launch_count": C.c_int64,
-             "blastgpu_dposv_mixed_workspace_bytes": C.c_size_t}
+             "blastgpu_dposv_mixed_workspace_bytes": C.c_size_t,
+             "blastgpu_dgesv_mixed_workspace_bytes": C.c_size_t}
 
 
 def lib() -> C.CDLL:

@@ -21,6 +21,8 @@
 //    thread per matrix. The backward substitution is a chain of dependent dot products in BLAST's
 //    order (each x_i starts from x_{i+1}); running it per thread keeps every lane busy while
 //    preserving that order.
+#include <math_constants.h>
+
 #include <atomic>
 
 #include "common.cuh"
@@ -30,11 +32,13 @@ namespace {
 
 constexpr int kWarps = 4;  // matrices (warps) per CTA of the getrf kernel
 
-struct GetrfItem {
-    double* a;
+template <typename T>
+struct GetrfItemT {
+    T* a;
     int m, n, lda;
     int32_t* ipiv;
 };
+using GetrfItem = GetrfItemT<double>;
 
 struct StridedGetrf {
     int m, n, lda;
@@ -56,47 +60,49 @@ struct DescGetrf {
 // First index of the largest |x|, rows [r0, r1) of column j, as BLAST's scalar scan would find:
 // a value replaces the running maximum only if strictly larger, so the first maximum wins and
 // NaN never wins unless it is the first element (then nothing replaces it).
-__device__ __forceinline__ int warp_iamax(const double* a, int lda, int r0, int r1, int j, int lane) {
-    double best = -1.0;
+template <typename T>
+__device__ __forceinline__ int warp_iamax(const T* a, int lda, int r0, int r1, int j, int lane) {
+    T best = (T)-1;
     int idx = 0x7fffffff;
     for (int r = r0 + lane; r < r1; r += 32) {
-        double const v = fabs(a[r + (int64_t)j * lda]);
+        T const v = fabs(a[r + (int64_t)j * lda]);
         if (v > best) { best = v; idx = r; }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-        double const ob = __shfl_xor_sync(0xffffffffu, best, off);
+        T const ob = __shfl_xor_sync(0xffffffffu, best, off);
         int const oi = __shfl_xor_sync(0xffffffffu, idx, off);
         if (ob > best || (ob == best && oi < idx)) { best = ob; idx = oi; }
     }
-    double const first = a[r0 + (int64_t)j * lda];
+    T const first = a[r0 + (int64_t)j * lda];
     if (first != first || idx == 0x7fffffff) idx = r0;  // NaN first element, or all NaN
     return idx - r0;
 }
 
 // getf2 (dense/Getf2.hpp:52-77) on the m x n block at (r0, c0); swaps cover the block's columns.
 // ipiv receives block-relative pivots. Returns the block-relative k+1 of a zero pivot, or 0.
-__device__ int warp_getf2(double* a, int lda, int r0, int c0, int m, int n, int32_t* ipiv, int lane) {
+template <typename T>
+__device__ int warp_getf2(T* a, int lda, int r0, int c0, int m, int n, int32_t* ipiv, int lane) {
     for (int k = 0; k < m && k < n; ++k) {
         int const ip = warp_iamax(a, lda, r0 + k, r0 + m, c0 + k, lane) + k;
         if (lane == 0) ipiv[k] = ip;
         if (ip != k) {
             for (int j = lane; j < n; j += 32) {
-                double* p = a + (int64_t)(c0 + j) * lda;
-                double const t = p[r0 + k];
+                T* p = a + (int64_t)(c0 + j) * lda;
+                T const t = p[r0 + k];
                 p[r0 + k] = p[r0 + ip];
                 p[r0 + ip] = t;
             }
         }
         __syncwarp();
-        double const piv = a[(r0 + k) + (int64_t)(c0 + k) * lda];
-        if (piv == 0.0) return k + 1;
-        double* col = a + (int64_t)(c0 + k) * lda;
+        T const piv = a[(r0 + k) + (int64_t)(c0 + k) * lda];
+        if (piv == (T)0) return k + 1;
+        T* col = a + (int64_t)(c0 + k) * lda;
         for (int i = k + 1 + lane; i < m; i += 32) col[r0 + i] = col[r0 + i] / piv;
         __syncwarp();
         for (int j = k + 1; j < n; ++j) {
-            double* cj = a + (int64_t)(c0 + j) * lda;
-            double const y = cj[r0 + k];
+            T* cj = a + (int64_t)(c0 + j) * lda;
+            T const y = cj[r0 + k];
             for (int i = k + 1 + lane; i < m; i += 32) cj[r0 + i] = fma(-col[r0 + i], y, cj[r0 + i]);
         }
         __syncwarp();
@@ -105,14 +111,15 @@ __device__ int warp_getf2(double* a, int lda, int r0, int c0, int m, int n, int3
 }
 
 // laswp on columns [c0, c1) with pivots ipiv[k0..k1) (dense/Laswp.hpp:37-43), lane per column.
-__device__ __forceinline__ void warp_laswp(double* a, int lda, int c0, int c1, int k0, int k1,
+template <typename T>
+__device__ __forceinline__ void warp_laswp(T* a, int lda, int c0, int c1, int k0, int k1,
                                            const int32_t* ipiv, int lane) {
     for (int j = c0 + lane; j < c1; j += 32) {
-        double* p = a + (int64_t)j * lda;
+        T* p = a + (int64_t)j * lda;
         for (int k = k0; k < k1; ++k) {
             int const q = ipiv[k];
             if (q != k) {
-                double const t = p[k];
+                T const t = p[k];
                 p[k] = p[q];
                 p[q] = t;
             }
@@ -120,10 +127,11 @@ __device__ __forceinline__ void warp_laswp(double* a, int lda, int c0, int c1, i
     }
 }
 
-__device__ int warp_getrf(GetrfItem it, int lane) {
+template <typename T>
+__device__ int warp_getrf(GetrfItemT<T> it, int lane) {
     constexpr int NB = 4;
     int const M = it.m, N = it.n, lda = it.lda;
-    double* a = it.a;
+    T* a = it.a;
     int32_t* ipiv = it.ipiv;
     int k = 0;
     for (; k + NB < M && k + NB < N; k += NB) {
@@ -137,11 +145,11 @@ __device__ int warp_getrf(GetrfItem it, int lane) {
         __syncwarp();
         // U12 := L11^{-1} A12, lane per column (trsm<Lower, unit>, scalar order).
         for (int j = k + NB + lane; j < N; j += 32) {
-            double* cj = a + (int64_t)j * lda;
-            double x[NB];
+            T* cj = a + (int64_t)j * lda;
+            T x[NB];
 #pragma unroll
             for (int i = 0; i < NB; ++i) {
-                double acc = cj[k + i];
+                T acc = cj[k + i];
 #pragma unroll
                 for (int q = 0; q < i; ++q) acc = fma(-a[(k + i) + (int64_t)(k + q) * lda], x[q], acc);
                 x[i] = acc;
@@ -154,11 +162,11 @@ __device__ int warp_getrf(GetrfItem it, int lane) {
         int const total = mr * nr;
         for (int e = lane; e < total; e += 32) {
             int const i = k + NB + e % mr, j = k + NB + e / mr;
-            double acc = 0.0;
+            T acc = (T)0;
 #pragma unroll
             for (int q = 0; q < NB; ++q) acc = fma(a[i + (int64_t)(k + q) * lda], a[(k + q) + (int64_t)j * lda], acc);
-            double* c = a + i + (int64_t)j * lda;
-            *c = fma(1.0, *c, -acc);
+            T* c = a + i + (int64_t)j * lda;
+            *c = fma((T)1, *c, -acc);
         }
         __syncwarp();
     }
@@ -183,10 +191,11 @@ constexpr int kCtaThreads = 256;
 
 constexpr int kPanelRows = 512;  // panels up to this height are factored in shared memory
 
-__device__ int cta_getrf(GetrfItem it, int* s_ret, double* sp) {
+template <typename T>
+__device__ int cta_getrf(GetrfItemT<T> it, int* s_ret, T* sp) {
     constexpr int NB = 4;
     int const M = it.m, N = it.n, lda = it.lda;
-    double* a = it.a;
+    T* a = it.a;
     int32_t* ipiv = it.ipiv;
     int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     int k = 0;
@@ -222,11 +231,11 @@ __device__ int cta_getrf(GetrfItem it, int* s_ret, double* sp) {
         // laswp on the other columns, thread per column
         for (int j = tid; j < N; j += kCtaThreads) {
             if (j >= k && j < k + NB) continue;
-            double* p = a + (int64_t)j * lda;
+            T* p = a + (int64_t)j * lda;
             for (int q = k; q < k + NB; ++q) {
                 int const pr = ipiv[q];
                 if (pr != q) {
-                    double const t = p[q];
+                    T const t = p[q];
                     p[q] = p[pr];
                     p[pr] = t;
                 }
@@ -235,11 +244,11 @@ __device__ int cta_getrf(GetrfItem it, int* s_ret, double* sp) {
         __syncthreads();
         // U12 := L11^{-1} A12, thread per column
         for (int j = k + NB + tid; j < N; j += kCtaThreads) {
-            double* cj = a + (int64_t)j * lda;
-            double x[NB];
+            T* cj = a + (int64_t)j * lda;
+            T x[NB];
 #pragma unroll
             for (int i = 0; i < NB; ++i) {
-                double acc = cj[k + i];
+                T acc = cj[k + i];
 #pragma unroll
                 for (int q = 0; q < i; ++q) acc = fma(-a[(k + i) + (int64_t)(k + q) * lda], x[q], acc);
                 x[i] = acc;
@@ -249,16 +258,16 @@ __device__ int cta_getrf(GetrfItem it, int* s_ret, double* sp) {
         __syncthreads();
         // A22 := A22 - A21 * U12, thread per row
         for (int i = k + NB + tid; i < M; i += kCtaThreads) {
-            double l[NB];
+            T l[NB];
 #pragma unroll
             for (int q = 0; q < NB; ++q) l[q] = a[i + (int64_t)(k + q) * lda];
             for (int j = k + NB; j < N; ++j) {
-                double const* u = a + k + (int64_t)j * lda;
-                double acc = 0.0;
+                T const* u = a + k + (int64_t)j * lda;
+                T acc = (T)0;
 #pragma unroll
                 for (int q = 0; q < NB; ++q) acc = fma(l[q], u[q], acc);
-                double* c = a + i + (int64_t)j * lda;
-                *c = fma(1.0, *c, -acc);
+                T* c = a + i + (int64_t)j * lda;
+                *c = fma((T)1, *c, -acc);
             }
         }
         __syncthreads();
@@ -274,11 +283,11 @@ __device__ int cta_getrf(GetrfItem it, int* s_ret, double* sp) {
         if (*s_ret) return k + *s_ret;
     }
     for (int j = tid; j < k; j += kCtaThreads) {
-        double* p = a + (int64_t)j * lda;
+        T* p = a + (int64_t)j * lda;
         for (int q = k; q < min(M, N); ++q) {
             int const pr = ipiv[q];
             if (pr != q) {
-                double const t = p[q];
+                T const t = p[q];
                 p[q] = p[pr];
                 p[pr] = t;
             }
@@ -799,6 +808,273 @@ int launch_getrs(Batch const& batch, int64_t count, int max_n, const int32_t* in
     return check_launch();
 }
 
+// ---------------------------------------------------------------------------------------------
+// Mixed-precision LU solve (blastgpu_dgesv_mixed_batched): binary32 factor, binary64 refinement.
+
+struct GesvMixedItems {
+    const blastgpu_gesv_mixed_desc* desc;
+    char* ws;
+    __device__ GetrfItemT<float> get(int64_t b) const {
+        blastgpu_gesv_mixed_desc const& d = desc[b];
+        int const n = d.A.rows;
+        return {reinterpret_cast<float*>(ws + d.ws_offset), n, n, n, d.ipiv};
+    }
+};
+
+// A (binary64) rounded to binary32 into the instance's scratch (leading dimension n), warp per
+// instance, lanes over rows.
+__global__ void __launch_bounds__(kWarps * 32) gesv_mixed_round_kernel(GesvMixedItems items, int64_t count) {
+    int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int64_t const b = (int64_t)blockIdx.x * kWarps + warp;
+    if (b >= count) return;
+    blastgpu_gesv_mixed_desc const& d = items.desc[b];
+    int const n = d.A.rows;
+    float* f = reinterpret_cast<float*>(items.ws + d.ws_offset);
+    for (int j = 0; j < n; ++j)
+        for (int i = lane; i < n; i += 32) f[i + (int64_t)j * n] = (float)d.A.data[i + (int64_t)j * d.A.ld];
+}
+
+__global__ void __launch_bounds__(kWarps * 32) getrf_warp_f32_kernel(GesvMixedItems items, int64_t count,
+                                                                      int32_t* info) {
+    int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int64_t const b = (int64_t)blockIdx.x * kWarps + warp;
+    if (b >= count) return;
+    int const r = warp_getrf(items.get(b), lane);
+    if (info && lane == 0) info[b] = r;
+}
+
+__global__ void __launch_bounds__(kCtaThreads) getrf_cta_f32_kernel(GesvMixedItems items, int64_t count,
+                                                                    int32_t* info) {
+    __shared__ int s_ret;
+    __shared__ float s_panel[4 * kPanelRows];
+    int64_t const b = blockIdx.x;
+    if (b >= count) return;
+    int const r = cta_getrf(items.get(b), &s_ret, s_panel);
+    if (info && threadIdx.x == 0) info[b] = r;
+}
+
+template <int MAXT, typename V>
+__device__ __forceinline__ V pick_t(V const (&v)[MAXT], int t) {
+    V r = (V)0;
+#pragma unroll
+    for (int q = 0; q < MAXT; ++q)
+        if (q == t) r = v[q];
+    return r;
+}
+
+template <int MAXT>
+__device__ __forceinline__ double warp_max_abs(double const (&v)[MAXT], int n, int lane) {
+    double m = 0.0;
+#pragma unroll
+    for (int t = 0; t < MAXT; ++t) {
+        double const a = fabs(v[t]);
+        if (lane + 32 * t < n) m = (a > m || a != a) ? a : m;  // NaN-propagating
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        double const o = __shfl_xor_sync(0xffffffffu, m, off);
+        m = (o > m || o != o) ? o : m;
+    }
+    return m;
+}
+
+// v := U^{-1} L^{-1} P v with the binary32 factor F (leading dimension n) of one instance, one warp,
+// lanes over rows (row lane + 32 t in v[t]). perm[i] is the row of v that row i of P v takes
+// (the pivots' interchanges composed), buf: n floats of shared memory. Both substitutions are
+// column sweeps: once an entry is final its lane broadcasts it, and every remaining row takes its
+// term; the factor's columns are read coalesced, one column ahead.
+template <int MAXT>
+__device__ void warp_lu_solve_f32(float (&v)[MAXT], const float* F, int n, const int* perm, float* buf, int lane) {
+#pragma unroll
+    for (int t = 0; t < MAXT; ++t)
+        if (lane + 32 * t < n) buf[lane + 32 * t] = v[t];
+    __syncwarp();
+#pragma unroll
+    for (int t = 0; t < MAXT; ++t) v[t] = lane + 32 * t < n ? buf[perm[lane + 32 * t]] : 0.f;
+    __syncwarp();
+    // forward: unit lower
+    float col[MAXT];
+#pragma unroll
+    for (int t = 0; t < MAXT; ++t) col[t] = (lane + 32 * t > 0 && lane + 32 * t < n) ? F[lane + 32 * t] : 0.f;
+    for (int l = 0; l + 1 < n; ++l) {
+        float nxt[MAXT];
+        const float* cn = F + (int64_t)(l + 1) * n;
+#pragma unroll
+        for (int t = 0; t < MAXT; ++t) {
+            int const i = lane + 32 * t;
+            nxt[t] = (i > l + 1 && i < n) ? cn[i] : 0.f;
+        }
+        float const vl = __shfl_sync(0xffffffffu, pick_t<MAXT>(v, l >> 5), l & 31);
+#pragma unroll
+        for (int t = 0; t < MAXT; ++t) {
+            int const i = lane + 32 * t;
+            if (i > l && i < n) v[t] = fmaf(-col[t], vl, v[t]);
+        }
+#pragma unroll
+        for (int t = 0; t < MAXT; ++t) col[t] = nxt[t];
+    }
+    // backward: upper, dividing by the diagonal
+    const float* cl = F + (int64_t)(n - 1) * n;
+#pragma unroll
+    for (int t = 0; t < MAXT; ++t) col[t] = (lane + 32 * t < n) ? cl[lane + 32 * t] : 0.f;
+    for (int l = n - 1; l >= 0; --l) {
+        float nxt[MAXT];
+        const float* cp = F + (int64_t)(l > 0 ? l - 1 : 0) * n;
+#pragma unroll
+        for (int t = 0; t < MAXT; ++t) {
+            int const i = lane + 32 * t;
+            nxt[t] = (l > 0 && i <= l - 1) ? cp[i] : 0.f;
+        }
+        int const tl = l >> 5;
+        // the owner divides its entry by u_ll (col holds column l, so its own row's entry is u_ll)
+#pragma unroll
+        for (int t = 0; t < MAXT; ++t)
+            if (lane + 32 * t == l) v[t] = v[t] / col[t];
+        float const xl = __shfl_sync(0xffffffffu, pick_t<MAXT>(v, tl), l & 31);
+#pragma unroll
+        for (int t = 0; t < MAXT; ++t) {
+            int const i = lane + 32 * t;
+            if (i < l) v[t] = fmaf(-col[t], xl, v[t]);
+        }
+#pragma unroll
+        for (int t = 0; t < MAXT; ++t) col[t] = nxt[t];
+    }
+}
+
+// Refinement, one warp per instance (n <= 32 MAXT): x0 from the binary32 factor, then r = b - A x
+// in binary64 (A read by columns, coalesced; |A|_inf from the same pass the first time), the
+// backward error, and corrections d = (U^{-1} L^{-1} P (r / |r|_inf)) |r|_inf until the error is at
+// most tol or max_iter corrections are spent. X overwrites B at the end.
+template <int MAXT>
+__global__ void __launch_bounds__(kWarps * 32) gesv_mixed_ir_kernel(GesvMixedItems items, int64_t count, double tol,
+                                                                   int max_iter, const int32_t* info, int32_t* iters,
+                                                                   double* berr) {
+    __shared__ double xs_all[kWarps][32 * MAXT];
+    __shared__ float buf_all[kWarps][32 * MAXT];
+    __shared__ int perm_all[kWarps][32 * MAXT];
+    int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int64_t const b = (int64_t)blockIdx.x * kWarps + warp;
+    if (b >= count) return;
+    blastgpu_gesv_mixed_desc const& d = items.desc[b];
+    int const n = d.A.rows, nrhs = d.B.cols;
+    if (n > 32 * MAXT) return;  // the launch's max_n bounds every instance
+    double* xs = xs_all[warp];
+    float* buf = buf_all[warp];
+    int* perm = perm_all[warp];
+    const float* F = reinterpret_cast<const float*>(items.ws + d.ws_offset);
+    if (info && info[b] != 0) {  // a zero binary32 pivot: no factor to refine with
+        for (int c = 0; c < nrhs; ++c)
+            for (int i = lane; i < n; i += 32) d.B.data[i + (int64_t)c * d.B.ld] = CUDART_NAN;
+        if (lane == 0) {
+            if (iters) iters[b] = 0;
+            if (berr) berr[b] = CUDART_NAN;
+        }
+        return;
+    }
+    // P as a permutation: the pivots' interchanges applied in order to the identity
+    for (int i = lane; i < n; i += 32) perm[i] = i;
+    __syncwarp();
+    if (lane == 0) {
+        for (int k = 0; k < n; ++k) {
+            int const q = d.ipiv[k];
+            if (q != k) {
+                int const t = perm[k];
+                perm[k] = perm[q];
+                perm[q] = t;
+            }
+        }
+    }
+    __syncwarp();
+    double anorm = -1.0, worst = 0.0;
+    int total_iters = 0;
+    for (int c = 0; c < nrhs; ++c) {
+        double* bc = d.B.data + (int64_t)c * d.B.ld;
+        double bv[MAXT], x[MAXT], r[MAXT];
+#pragma unroll
+        for (int t = 0; t < MAXT; ++t) bv[t] = lane + 32 * t < n ? bc[lane + 32 * t] : 0.0;
+        double const bnorm = warp_max_abs<MAXT>(bv, n, lane);
+        float w[MAXT];
+#pragma unroll
+        for (int t = 0; t < MAXT; ++t) w[t] = (float)bv[t];
+        warp_lu_solve_f32<MAXT>(w, F, n, perm, buf, lane);
+#pragma unroll
+        for (int t = 0; t < MAXT; ++t) x[t] = (double)w[t];
+        double be = CUDART_NAN;
+        int it = 0;
+        while (true) {
+            // r = b - A x
+#pragma unroll
+            for (int t = 0; t < MAXT; ++t)
+                if (lane + 32 * t < n) xs[lane + 32 * t] = x[t];
+            __syncwarp();
+            double rs[MAXT];
+#pragma unroll
+            for (int t = 0; t < MAXT; ++t) {
+                r[t] = bv[t];
+                rs[t] = 0.0;
+            }
+            bool const first = anorm < 0.0;
+            const double* A = d.A.data;
+            double acol[MAXT];
+#pragma unroll
+            for (int t = 0; t < MAXT; ++t) acol[t] = lane + 32 * t < n ? A[lane + 32 * t] : 0.0;
+            for (int j = 0; j < n; ++j) {
+                double anx[MAXT];  // column j + 1, loaded before column j's FMAs
+                const double* an = A + (int64_t)(j + 1 < n ? j + 1 : j) * d.A.ld;
+#pragma unroll
+                for (int t = 0; t < MAXT; ++t) anx[t] = lane + 32 * t < n ? an[lane + 32 * t] : 0.0;
+                double const xj = xs[j];
+#pragma unroll
+                for (int t = 0; t < MAXT; ++t) {
+                    r[t] = fma(-acol[t], xj, r[t]);
+                    if (first) rs[t] += fabs(acol[t]);
+                }
+#pragma unroll
+                for (int t = 0; t < MAXT; ++t) acol[t] = anx[t];
+            }
+            __syncwarp();
+            if (first) anorm = warp_max_abs<MAXT>(rs, n, lane);
+            double const rm = warp_max_abs<MAXT>(r, n, lane);
+            double const xm = warp_max_abs<MAXT>(x, n, lane);
+            double const den = anorm * xm + bnorm;
+            be = den > 0.0 ? rm / den : (rm == 0.0 ? 0.0 : CUDART_INF);
+            if (!(be > tol) || it >= max_iter) break;
+#pragma unroll
+            for (int t = 0; t < MAXT; ++t) w[t] = (float)(r[t] / rm);
+            warp_lu_solve_f32<MAXT>(w, F, n, perm, buf, lane);
+#pragma unroll
+            for (int t = 0; t < MAXT; ++t) x[t] += (double)w[t] * rm;
+            ++it;
+        }
+#pragma unroll
+        for (int t = 0; t < MAXT; ++t)
+            if (lane + 32 * t < n) bc[lane + 32 * t] = x[t];
+        total_iters = max(total_iters, it);
+        worst = (be > worst || be != be) ? be : worst;
+    }
+    if (lane == 0) {
+        if (iters) iters[b] = total_iters;
+        if (berr) berr[b] = worst;
+    }
+}
+
+int launch_gesv_mixed(GesvMixedItems items, int64_t count, int max_n, double tol, int max_iter, int32_t* info,
+                      int32_t* iters, double* berr, cudaStream_t s) {
+    if (count == 0) return BLASTGPU_SUCCESS;
+    int64_t const wblocks = (count + kWarps - 1) / kWarps;
+    if (wblocks > 0x7fffffff || count > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
+    unsigned const wg = (unsigned)wblocks;
+    gesv_mixed_round_kernel<<<wg, kWarps * 32, 0, s>>>(items, count);
+    if (max_n > 64) getrf_cta_f32_kernel<<<(unsigned)count, kCtaThreads, 0, s>>>(items, count, info);
+    else getrf_warp_f32_kernel<<<wg, kWarps * 32, 0, s>>>(items, count, info);
+    int const maxt = (max_n + 31) / 32;
+    if (maxt <= 1) gesv_mixed_ir_kernel<1><<<wg, kWarps * 32, 0, s>>>(items, count, tol, max_iter, info, iters, berr);
+    else if (maxt <= 2) gesv_mixed_ir_kernel<2><<<wg, kWarps * 32, 0, s>>>(items, count, tol, max_iter, info, iters, berr);
+    else if (maxt <= 4) gesv_mixed_ir_kernel<4><<<wg, kWarps * 32, 0, s>>>(items, count, tol, max_iter, info, iters, berr);
+    else gesv_mixed_ir_kernel<8><<<wg, kWarps * 32, 0, s>>>(items, count, tol, max_iter, info, iters, berr);
+    return check_launch();
+}
+
 }  // namespace
 }  // namespace blastgpu
 
@@ -866,6 +1142,27 @@ int blastgpu_dgesv_batched(const blastgpu_getrf_desc* desc, int32_t* info, int64
     int st = blastgpu_dgetrf_batched(desc, info, batch, max_n, stream);
     if (st != BLASTGPU_SUCCESS) return st;
     return blastgpu_dgetrs_batched(desc, info, batch, max_n, stream);
+}
+
+size_t blastgpu_dgesv_mixed_workspace_bytes(int n) {
+    if (n <= 0) return 0;
+    return (((size_t)n * n * sizeof(float)) + 255) / 256 * 256;
+}
+
+int blastgpu_dgesv_mixed_batched(const blastgpu_gesv_mixed_desc* desc, int64_t batch, int max_n, void* workspace,
+                                 double tol, int max_iter, int32_t* info, int32_t* iters, double* berr,
+                                 blastgpu_stream_t stream) {
+    if (batch < 0) return -2;
+    if (batch == 0) return BLASTGPU_SUCCESS;
+    if (!desc) return -1;
+    if (max_n < 0) return -3;
+    if (max_n > 256) return BLASTGPU_ERR_TOO_LARGE;
+    if (!workspace) return -4;
+    if (!(tol >= 0.0)) return -5;
+    if (max_iter < 0) return -6;
+    if (!info) return -7;  // the refinement reads the factorisation's info
+    return launch_gesv_mixed(GesvMixedItems{desc, static_cast<char*>(workspace)}, batch, max_n, tol, max_iter,
+                             info, iters, berr, as_cuda(stream));
 }
 
 }  // extern "C"

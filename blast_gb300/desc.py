@@ -20,6 +20,10 @@ assert GEMM_DTYPE.itemsize == 144
 GETRF_DTYPE = np.dtype([("A", MAT_DTYPE), ("ipiv", "<u8"), ("B", MAT_DTYPE)], align=True)
 assert GETRF_DTYPE.itemsize == 72
 
+GESV_MIXED_DTYPE = np.dtype([("A", MAT_DTYPE), ("ipiv", "<u8"), ("B", MAT_DTYPE), ("ws_offset", "<i8")],
+                            align=True)
+assert GESV_MIXED_DTYPE.itemsize == 80
+
 POSV_DTYPE = np.dtype([("A", MAT_DTYPE), ("L", MAT_DTYPE), ("B", MAT_DTYPE), ("X", MAT_DTYPE),
                        ("ws_offset", "<i8")], align=True)
 assert POSV_DTYPE.itemsize == 136

@@ -161,6 +161,77 @@ def capture_graph(fn):
     return g
 
 
+class MixedGesvPlan:
+    """Ragged batch of mixed-precision LU solves (blastgpu_dgesv_mixed_batched): A_i (n_i x n_i,
+    binary64, left untouched) rounded to binary32 and factored with partial pivoting, then
+    X_i = A_i^{-1} B_i (written over B_i) refined in binary64 to a normwise backward error <= tol.
+    n_i <= 256. Two size bins (n > 64: one CTA per factorisation; n <= 64: one warp) run on forked
+    streams; the refinement is one warp per matrix."""
+
+    def __init__(self, A: Packed, B: Packed, tol=1e-12, max_iter=10):
+        n = A.rows
+        if np.any(A.cols != n) or np.any(B.rows != n):
+            raise ValueError("Invalid argument size")
+        self.count = len(n)
+        if self.count and int(n.max()) > 256:
+            raise ValueError("n > 256 is not supported by the mixed-precision LU solve")
+        self.tol, self.max_iter = float(tol), int(max_iter)
+        device = A.buf.device
+        self.order = np.argsort(-n, kind="stable")
+        self.ipiv = Packed(n, np.ones_like(n), device, dtype=torch.int32)
+        per = np.array([_lib.lib().blastgpu_dgesv_mixed_workspace_bytes(int(k)) for k in n], dtype=np.int64)
+        ws_off = np.zeros(self.count, dtype=np.int64)
+        if self.count:
+            ws_off[self.order] = np.concatenate([[0], np.cumsum(per[self.order])[:-1]])
+        self.workspace = torch.empty(max(int(per.sum()), 256), dtype=torch.uint8, device=device)
+        recs = np.zeros(self.count, dtype=desc.GESV_MIXED_DTYPE)
+        for slot, i in enumerate(self.order):
+            recs[slot] = (A.record(i), self.ipiv.ptr(i), B.record(i), int(ws_off[i]))
+        self.d = desc.upload(recs, device)
+        self.info = torch.zeros(self.count, dtype=torch.int32, device=device)
+        self.iters = torch.zeros(self.count, dtype=torch.int32, device=device)
+        self.berr = torch.zeros(self.count, dtype=torch.float64, device=device)
+        self._keep = (A, B)
+        sorted_n = n[self.order]
+        big = int(np.sum(sorted_n > 64))
+        self.bins = [(b0, b1, int(sorted_n[b0])) for b0, b1 in ((0, big), (big, self.count)) if b1 > b0]
+        self.side = torch.cuda.Stream(device)
+
+    def _launch(self, b0, b1, max_n, s):
+        _lib.call("blastgpu_dgesv_mixed_batched", self.d.data_ptr() + b0 * desc.GESV_MIXED_DTYPE.itemsize,
+                  b1 - b0, max_n, self.workspace.data_ptr(), self.tol, self.max_iter,
+                  self.info.data_ptr() + 4 * b0, self.iters.data_ptr() + 4 * b0, self.berr.data_ptr() + 8 * b0, s)
+
+    def run(self, stream=None):
+        cur = stream or torch.cuda.current_stream()
+        if not self.bins:
+            return
+        if len(self.bins) == 2:
+            start = torch.cuda.Event()
+            start.record(cur)
+            self.side.wait_event(start)
+            self._launch(*self.bins[1], self.side.cuda_stream)
+        self._launch(*self.bins[0], cur.cuda_stream)
+        if len(self.bins) == 2:
+            done = torch.cuda.Event()
+            done.record(self.side)
+            cur.wait_event(done)
+
+    def capture(self):
+        """Records run() into a CUDA graph; returns the torch.cuda.CUDAGraph (call .replay())."""
+        return capture_graph(self.run)
+
+    def pivots(self):
+        host = self.ipiv.buf.cpu().numpy()
+        return [host[int(o):int(o) + int(k)] for o, k in zip(self.ipiv.offsets, self.ipiv.rows)]
+
+    def results(self):
+        """(info, corrections, backward error) per instance, in the caller's order."""
+        inv = np.empty_like(self.order)
+        inv[self.order] = np.arange(self.count)
+        return (self.info.cpu().numpy()[inv], self.iters.cpu().numpy()[inv], self.berr.cpu().numpy()[inv])
+
+
 class GesvPlan:
     """Ragged batch of LU solves (getrf + getrs), column-major A_i (n_i x n_i), B_i (n_i x r_i)."""
 

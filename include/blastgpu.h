@@ -308,6 +308,29 @@ int blastgpu_dgetrs_batched(const blastgpu_getrf_desc* desc, const int32_t* info
 int blastgpu_dgesv_batched(const blastgpu_getrf_desc* desc, int32_t* info, int64_t batch,
                            int max_n, blastgpu_stream_t stream);
 
+/* Mixed-precision LU solve with iterative refinement (no BLAST counterpart; the benchmark spec's
+ * mixed form applied to getrf/getrs): per instance, A (binary64, read only) is rounded to
+ * binary32 in the caller's workspace and factored there by the same blocked partial-pivoting
+ * algorithm as blastgpu_dgetrf_batched; X := A^{-1} B (B overwritten) is then refined in binary64
+ * (r = b - A x, correction solved with the binary32 factor on r / |r|_inf) until the normwise
+ * backward error |r|_inf / (|A|_inf |x|_inf + |b|_inf) <= tol or max_iter corrections. Square
+ * matrices with n <= 256. Per instance: info (0, or k+1 of an exactly zero binary32 pivot; such
+ * instances get X = NaN and berr = NaN and should be solved with blastgpu_dgesv_batched), iters
+ * (corrections, the most over the right-hand sides) and berr (the largest backward error). The
+ * pivots are the binary32 factorisation's and may differ from the binary64 ones. */
+typedef struct blastgpu_gesv_mixed_desc {
+    blastgpu_mat A;     /* n x n general matrix, column-major, binary64; not written */
+    int32_t* ipiv;      /* n pivots of the binary32 factorisation (0-based, absolute) */
+    blastgpu_mat B;     /* n x nrhs column-major right-hand sides; overwritten by X */
+    int64_t ws_offset;  /* byte offset of this instance's scratch in `workspace`
+                           (blastgpu_dgesv_mixed_workspace_bytes(n) bytes, 4-byte aligned) */
+} blastgpu_gesv_mixed_desc;   /* 80 bytes */
+
+size_t blastgpu_dgesv_mixed_workspace_bytes(int n);
+int blastgpu_dgesv_mixed_batched(const blastgpu_gesv_mixed_desc* desc, int64_t batch, int max_n, void* workspace,
+                                 double tol, int max_iter, int32_t* info, int32_t* iters, double* berr,
+                                 blastgpu_stream_t stream);
+
 /* ---------------------------------------------------------------------------------------------
  * Ragged Cholesky solves, n <= 512, one CTA per matrix, one launch for the whole batch.
  * Per instance: potrf(A, L) (lower triangle of A read), then X = A^{-1} B (X may alias B).

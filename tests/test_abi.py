@@ -171,6 +171,7 @@ def test_descriptor_layouts_match_header(tmp_path):
         "blastgpu_mat": (desc.MAT_DTYPE, ["data", "rows", "cols", "ld", "layout", "ps", "reserved"]),
         "blastgpu_gemm_desc": (desc.GEMM_DTYPE, ["A", "B", "C", "D", "alpha", "beta"]),
         "blastgpu_getrf_desc": (desc.GETRF_DTYPE, ["A", "ipiv", "B"]),
+        "blastgpu_gesv_mixed_desc": (desc.GESV_MIXED_DTYPE, ["A", "ipiv", "B", "ws_offset"]),
         "blastgpu_posv_desc": (desc.POSV_DTYPE, ["A", "L", "B", "X", "ws_offset"]),
         "blastgpu_posv_bwd_desc": (desc.POSV_BWD_DTYPE, ["A", "L", "X", "Xbar", "Bbar", "Abar"]),
         "blastgpu_potrf_desc": (desc.POTRF_DTYPE, ["A", "L"]),

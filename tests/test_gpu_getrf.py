@@ -7,7 +7,7 @@ with no near-tie exceptions needed.
 import numpy as np
 import pytest
 
-from helpers import approx_equal, to_dev
+from helpers import approx_equal, normwise, to_dev
 
 pytestmark = pytest.mark.gpu
 
@@ -301,3 +301,72 @@ def test_getrf_left_looking_singular_and_ties(gpu, oracle_lib):
     LUs = np.asfortranarray(sing.copy())
     ps = np.zeros(n, dtype=np.int32)
     assert info[1] == oracle_lib.getrf(LUs, ps) == 78
+
+
+def _berr(A, x, b):
+    r = b - A @ x
+    return float(np.abs(r).max() / (np.abs(A).sum(1).max() * np.abs(x).max() + np.abs(b).max()))
+
+
+@pytest.mark.parametrize("count,seed", [(300, 5), (64, 6)])
+def test_mixed_gesv_refines_to_tolerance(gpu, count, seed):
+    """Mixed-precision LU (binary32 factor, binary64 refinement) on the ragged LU workload's
+    distribution (n log-uniform in [4, 256], N(0,1) entries) plus the edge sizes 1, 2, 32, 33, 64,
+    65 and 256, with 1 to 3 right-hand sides: every instance converges to a normwise backward error
+    <= 1e-12, recomputed here in binary64; the solutions agree with LAPACK's within the
+    conditioning; A is left untouched and B holds X."""
+    import scipy.linalg as sla
+    import torch
+
+    from blast_gb300.ragged import MixedGesvPlan, Packed
+
+    rng = np.random.default_rng(seed)
+    ns = np.floor(np.exp(rng.uniform(np.log(4), np.log(257), count))).astype(int)
+    ns = np.concatenate([ns, [1, 2, 32, 33, 64, 65, 256]])
+    rs = 1 + rng.integers(0, 3, len(ns))
+    As = [rng.standard_normal((n, n)) for n in ns]
+    Bs = [rng.standard_normal((n, r)) for n, r in zip(ns, rs)]
+    A = Packed(ns, ns, "cuda")
+    A.fill_from(As)
+    B = Packed(ns, rs, "cuda")
+    B.fill_from(Bs)
+    A0 = A.buf.clone()
+    plan = MixedGesvPlan(A, B, tol=1e-12, max_iter=10)
+    plan.run()
+    torch.cuda.synchronize()
+    info, iters, berr = plan.results()
+    assert not info.any()
+    assert np.all(berr <= 1e-12), berr.max()
+    assert torch.equal(A.buf, A0)
+    for n, Ah, Bh, Xg in zip(ns, As, Bs, B.to_list()):
+        assert _berr(Ah, Xg, Bh) <= 1.05e-12, n
+        Xr = sla.solve(Ah, Bh)
+        cond = np.linalg.cond(Ah, np.inf)
+        assert normwise(Xg, Xr) <= 1e-12 * cond * 10, (n, normwise(Xg, Xr), cond)
+    assert iters.max() <= 10
+
+
+def test_mixed_gesv_zero_pivot_reported(gpu):
+    """An instance whose binary32 factorisation meets an exactly zero pivot reports info = k + 1,
+    gets X = NaN and a NaN backward error; the other instances of the batch are solved."""
+    import torch
+
+    from blast_gb300.ragged import MixedGesvPlan, Packed
+
+    rng = np.random.default_rng(8)
+    ns = [40, 100, 7, 130]
+    As = [rng.standard_normal((n, n)) for n in ns]
+    As[1][:, 5] = 0.0  # column 5 is zero: the sixth pivot is exactly zero
+    Bs = [rng.standard_normal((n, 1)) for n in ns]
+    A = Packed(ns, ns, "cuda")
+    A.fill_from(As)
+    B = Packed(ns, [1] * len(ns), "cuda")
+    B.fill_from(Bs)
+    plan = MixedGesvPlan(A, B)
+    plan.run()
+    torch.cuda.synchronize()
+    info, iters, berr = plan.results()
+    assert info[1] == 6 and np.isnan(berr[1]) and np.all(np.isnan(B.to_list()[1]))
+    for i in (0, 2, 3):
+        assert info[i] == 0 and berr[i] <= 1e-12
+        assert _berr(As[i], B.to_list()[i], Bs[i]) <= 1.05e-12
