@@ -329,16 +329,17 @@ __global__ void __launch_bounds__(kCtaThreads) getrf_cta_kernel(Batch batch, int
 // memory, and at the end every column left of a step takes that step's swaps, in step order.
 constexpr int kLazyCols = 32;
 
-__device__ __forceinline__ void lazy_apply_step(double* sp, int ld, int n, int k, int j, const double* L,
+template <typename T>
+__device__ __forceinline__ void lazy_apply_step(T* sp, int ld, int n, int k, int j, const T* L,
                                                 int lda, const int32_t* ipiv, int lane) {
-    double* col = sp + (int64_t)j * ld;
+    T* col = sp + (int64_t)j * ld;
     // swaps of step k (rows k..k+3), one lane
     if (lane == 0) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             int const pr = ipiv[k + q];
             if (pr != k + q) {
-                double const t = col[k + q];
+                T const t = col[k + q];
                 col[k + q] = col[pr];
                 col[pr] = t;
             }
@@ -346,10 +347,10 @@ __device__ __forceinline__ void lazy_apply_step(double* sp, int ld, int n, int k
     }
     __syncwarp();
     // rows k..k+3 of U (trsm<Lower, unit> with L(k:k+4, k:k+4)), computed by every lane
-    double x[4];
+    T x[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        double acc = col[k + i];
+        T acc = col[k + i];
 #pragma unroll
         for (int q = 0; q < i; ++q) acc = fma(-L[(k + i) + (int64_t)(k + q) * lda], x[q], acc);
         x[i] = acc;
@@ -358,35 +359,36 @@ __device__ __forceinline__ void lazy_apply_step(double* sp, int ld, int n, int k
     if (lane < 4) col[k + lane] = lane == 0 ? x[0] : lane == 1 ? x[1] : lane == 2 ? x[2] : x[3];
     // rank-4 update of the rows below, lanes over rows
     for (int i = k + 4 + lane; i < n; i += 32) {
-        double acc = 0.0;
+        T acc = (T)0;
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc = fma(L[i + (int64_t)(k + q) * lda], x[q], acc);
-        col[i] = fma(1.0, col[i], -acc);
+        col[i] = fma((T)1, col[i], -acc);
     }
     __syncwarp();
 }
 
 // The same step applied within the super-panel (L block in shared memory, column c of sp).
-__device__ __forceinline__ void lazy_apply_step_smem(double* sp, int ld, int n, int k, int kc, int c,
+template <typename T>
+__device__ __forceinline__ void lazy_apply_step_smem(T* sp, int ld, int n, int k, int kc, int c,
                                                      const int32_t* ipiv, int lane) {
-    double* col = sp + (int64_t)c * ld;
-    double const* Lk = sp + (int64_t)kc * ld;  // column k of the matrix is column kc of the super-panel
+    T* col = sp + (int64_t)c * ld;
+    T const* Lk = sp + (int64_t)kc * ld;  // column k of the matrix is column kc of the super-panel
     if (lane == 0) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             int const pr = ipiv[k + q];
             if (pr != k + q) {
-                double const t = col[k + q];
+                T const t = col[k + q];
                 col[k + q] = col[pr];
                 col[pr] = t;
             }
         }
     }
     __syncwarp();
-    double x[4];
+    T x[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        double acc = col[k + i];
+        T acc = col[k + i];
 #pragma unroll
         for (int q = 0; q < i; ++q) acc = fma(-Lk[(k + i) + (int64_t)q * ld], x[q], acc);
         x[i] = acc;
@@ -394,18 +396,19 @@ __device__ __forceinline__ void lazy_apply_step_smem(double* sp, int ld, int n, 
     __syncwarp();
     if (lane < 4) col[k + lane] = lane == 0 ? x[0] : lane == 1 ? x[1] : lane == 2 ? x[2] : x[3];
     for (int i = k + 4 + lane; i < n; i += 32) {
-        double acc = 0.0;
+        T acc = (T)0;
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc = fma(Lk[i + (int64_t)q * ld], x[q], acc);
-        col[i] = fma(1.0, col[i], -acc);
+        col[i] = fma((T)1, col[i], -acc);
     }
     __syncwarp();
 }
 
-__device__ int cta_getrf_lazy(GetrfItem it, int* s_ret, double* sp) {
+template <typename T>
+__device__ int cta_getrf_lazy(GetrfItemT<T> it, int* s_ret, T* sp) {
     constexpr int NB = 4;
     int const n = it.n, lda = it.lda, ld = n | 1;
-    double* a = it.a;
+    T* a = it.a;
     int32_t* ipiv = it.ipiv;
     int const tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     int const nwarps = kCtaThreads / 32;
@@ -449,11 +452,11 @@ __device__ int cta_getrf_lazy(GetrfItem it, int* s_ret, double* sp) {
     // the swaps of every step on the columns left of it, in step order (BLAST's laswp of the
     // left columns at each step, and the final one after the remainder)
     for (int c = tid; c < n; c += kCtaThreads) {
-        double* col = a + (int64_t)c * lda;
+        T* col = a + (int64_t)c * lda;
         for (int k = (c / NB + 1) * NB; k < n; ++k) {
             int const pr = ipiv[k];
             if (pr != k) {
-                double const t = col[k];
+                T const t = col[k];
                 col[k] = col[pr];
                 col[pr] = t;
             }
@@ -821,17 +824,18 @@ struct GesvMixedItems {
     }
 };
 
-// A (binary64) rounded to binary32 into the instance's scratch (leading dimension n), warp per
-// instance, lanes over rows.
-__global__ void __launch_bounds__(kWarps * 32) gesv_mixed_round_kernel(GesvMixedItems items, int64_t count) {
-    int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int64_t const b = (int64_t)blockIdx.x * kWarps + warp;
+// A (binary64) rounded to binary32 into the instance's scratch (leading dimension n), one CTA of
+// 256 threads per instance, consecutive threads on consecutive elements of a column.
+__global__ void __launch_bounds__(kCtaThreads) gesv_mixed_round_kernel(GesvMixedItems items, int64_t count) {
+    int64_t const b = blockIdx.x;
     if (b >= count) return;
     blastgpu_gesv_mixed_desc const& d = items.desc[b];
-    int const n = d.A.rows;
+    int const n = d.A.rows, nn = n * n;
     float* f = reinterpret_cast<float*>(items.ws + d.ws_offset);
-    for (int j = 0; j < n; ++j)
-        for (int i = lane; i < n; i += 32) f[i + (int64_t)j * n] = (float)d.A.data[i + (int64_t)j * d.A.ld];
+    for (int e = threadIdx.x; e < nn; e += kCtaThreads) {
+        int const j = e / n, i = e - j * n;
+        f[e] = (float)d.A.data[i + (int64_t)j * d.A.ld];
+    }
 }
 
 __global__ void __launch_bounds__(kWarps * 32) getrf_warp_f32_kernel(GesvMixedItems items, int64_t count,
@@ -850,6 +854,19 @@ __global__ void __launch_bounds__(kCtaThreads) getrf_cta_f32_kernel(GesvMixedIte
     int64_t const b = blockIdx.x;
     if (b >= count) return;
     int const r = cta_getrf(items.get(b), &s_ret, s_panel);
+    if (info && threadIdx.x == 0) info[b] = r;
+}
+
+// The left-looking schedule in binary32 (super-panels of 32 columns, n x 32 floats of dynamic
+// shared memory): far less traffic to L2 than the right-looking kernel's read-modify-write of the
+// trailing matrix at every step.
+__global__ void __launch_bounds__(kCtaThreads) getrf_cta_lazy_f32_kernel(GesvMixedItems items, int64_t count,
+                                                                         int32_t* info) {
+    extern __shared__ float spf[];
+    __shared__ int s_ret;
+    int64_t const b = blockIdx.x;
+    if (b >= count) return;
+    int const r = cta_getrf_lazy(items.get(b), &s_ret, spf);
     if (info && threadIdx.x == 0) info[b] = r;
 }
 
@@ -882,7 +899,21 @@ __device__ __forceinline__ double warp_max_abs(double const (&v)[MAXT], int n, i
 // lanes over rows (row lane + 32 t in v[t]). perm[i] is the row of v that row i of P v takes
 // (the pivots' interchanges composed), buf: n floats of shared memory. Both substitutions are
 // column sweeps: once an entry is final its lane broadcasts it, and every remaining row takes its
-// term; the factor's columns are read coalesced, one column ahead.
+// term. The factor's columns are read coalesced into four register slots, each reloaded with the
+// column four steps ahead right after use, so a load has three steps to arrive.
+template <int MAXT>
+struct ColSlots {
+    float v[4][MAXT];
+    // rows lo <= i < hi of column c (zeros elsewhere, or for c outside [0, n))
+    __device__ __forceinline__ void load(int s, const float* F, int n, int c, int lo, int hi, int lane) {
+#pragma unroll
+        for (int t = 0; t < MAXT; ++t) {
+            int const i = lane + 32 * t;
+            v[s][t] = (c >= 0 && c < n && i >= lo && i < hi) ? F[i + (int64_t)c * n] : 0.f;
+        }
+    }
+};
+
 template <int MAXT>
 __device__ void warp_lu_solve_f32(float (&v)[MAXT], const float* F, int n, const int* perm, float* buf, int lane) {
 #pragma unroll
@@ -892,52 +923,46 @@ __device__ void warp_lu_solve_f32(float (&v)[MAXT], const float* F, int n, const
 #pragma unroll
     for (int t = 0; t < MAXT; ++t) v[t] = lane + 32 * t < n ? buf[perm[lane + 32 * t]] : 0.f;
     __syncwarp();
-    // forward: unit lower
-    float col[MAXT];
+    ColSlots<MAXT> cs;
+    // forward: unit lower; step l uses column l below the diagonal
 #pragma unroll
-    for (int t = 0; t < MAXT; ++t) col[t] = (lane + 32 * t > 0 && lane + 32 * t < n) ? F[lane + 32 * t] : 0.f;
-    for (int l = 0; l + 1 < n; ++l) {
-        float nxt[MAXT];
-        const float* cn = F + (int64_t)(l + 1) * n;
+    for (int s = 0; s < 4; ++s) cs.load(s, F, n, s, s + 1, n, lane);
+    for (int l0 = 0; l0 < n - 1; l0 += 4) {
 #pragma unroll
-        for (int t = 0; t < MAXT; ++t) {
-            int const i = lane + 32 * t;
-            nxt[t] = (i > l + 1 && i < n) ? cn[i] : 0.f;
+        for (int s = 0; s < 4; ++s) {
+            int const l = l0 + s;
+            if (l < n - 1) {
+                float const vl = __shfl_sync(0xffffffffu, pick_t<MAXT>(v, l >> 5), l & 31);
+#pragma unroll
+                for (int t = 0; t < MAXT; ++t) {
+                    int const i = lane + 32 * t;
+                    if (i > l && i < n) v[t] = fmaf(-cs.v[s][t], vl, v[t]);
+                }
+            }
+            cs.load(s, F, n, l + 4, l + 5, n, lane);
         }
-        float const vl = __shfl_sync(0xffffffffu, pick_t<MAXT>(v, l >> 5), l & 31);
-#pragma unroll
-        for (int t = 0; t < MAXT; ++t) {
-            int const i = lane + 32 * t;
-            if (i > l && i < n) v[t] = fmaf(-col[t], vl, v[t]);
-        }
-#pragma unroll
-        for (int t = 0; t < MAXT; ++t) col[t] = nxt[t];
     }
-    // backward: upper, dividing by the diagonal
-    const float* cl = F + (int64_t)(n - 1) * n;
+    // backward: upper, dividing by the diagonal; step l uses column l on and above the diagonal
 #pragma unroll
-    for (int t = 0; t < MAXT; ++t) col[t] = (lane + 32 * t < n) ? cl[lane + 32 * t] : 0.f;
-    for (int l = n - 1; l >= 0; --l) {
-        float nxt[MAXT];
-        const float* cp = F + (int64_t)(l > 0 ? l - 1 : 0) * n;
+    for (int s = 0; s < 4; ++s) cs.load(s, F, n, n - 1 - s, 0, n - s, lane);
+    for (int l0 = n - 1; l0 >= 0; l0 -= 4) {
 #pragma unroll
-        for (int t = 0; t < MAXT; ++t) {
-            int const i = lane + 32 * t;
-            nxt[t] = (l > 0 && i <= l - 1) ? cp[i] : 0.f;
+        for (int s = 0; s < 4; ++s) {
+            int const l = l0 - s;
+            if (l >= 0) {
+                // the owner divides its entry by u_ll (slot s holds column l, so its own row's entry is u_ll)
+#pragma unroll
+                for (int t = 0; t < MAXT; ++t)
+                    if (lane + 32 * t == l) v[t] = v[t] / cs.v[s][t];
+                float const xl = __shfl_sync(0xffffffffu, pick_t<MAXT>(v, l >> 5), l & 31);
+#pragma unroll
+                for (int t = 0; t < MAXT; ++t) {
+                    int const i = lane + 32 * t;
+                    if (i < l) v[t] = fmaf(-cs.v[s][t], xl, v[t]);
+                }
+            }
+            cs.load(s, F, n, l - 4, 0, l - 3, lane);
         }
-        int const tl = l >> 5;
-        // the owner divides its entry by u_ll (col holds column l, so its own row's entry is u_ll)
-#pragma unroll
-        for (int t = 0; t < MAXT; ++t)
-            if (lane + 32 * t == l) v[t] = v[t] / col[t];
-        float const xl = __shfl_sync(0xffffffffu, pick_t<MAXT>(v, tl), l & 31);
-#pragma unroll
-        for (int t = 0; t < MAXT; ++t) {
-            int const i = lane + 32 * t;
-            if (i < l) v[t] = fmaf(-col[t], xl, v[t]);
-        }
-#pragma unroll
-        for (int t = 0; t < MAXT; ++t) col[t] = nxt[t];
     }
 }
 
@@ -945,26 +970,21 @@ __device__ void warp_lu_solve_f32(float (&v)[MAXT], const float* F, int n, const
 // in binary64 (A read by columns, coalesced; |A|_inf from the same pass the first time), the
 // backward error, and corrections d = (U^{-1} L^{-1} P (r / |r|_inf)) |r|_inf until the error is at
 // most tol or max_iter corrections are spent. X overwrites B at the end.
+// One instance with n <= 32 MAXT (its own row-block count, so that blocks past its last row
+// cost nothing); xs, buf, perm: n doubles, floats and ints of the warp's shared memory.
 template <int MAXT>
-__global__ void __launch_bounds__(kWarps * 32) gesv_mixed_ir_kernel(GesvMixedItems items, int64_t count, double tol,
-                                                                   int max_iter, const int32_t* info, int32_t* iters,
-                                                                   double* berr) {
-    __shared__ double xs_all[kWarps][32 * MAXT];
-    __shared__ float buf_all[kWarps][32 * MAXT];
-    __shared__ int perm_all[kWarps][32 * MAXT];
-    int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int64_t const b = (int64_t)blockIdx.x * kWarps + warp;
-    if (b >= count) return;
+__device__ void gesv_mixed_ir(GesvMixedItems const& items, int64_t b, double tol, int max_iter, const int32_t* info,
+                              int32_t* iters, double* berr, double* xs, float* buf, int* perm, int lane) {
+    // the descriptor's fields, read once
     blastgpu_gesv_mixed_desc const& d = items.desc[b];
-    int const n = d.A.rows, nrhs = d.B.cols;
-    if (n > 32 * MAXT) return;  // the launch's max_n bounds every instance
-    double* xs = xs_all[warp];
-    float* buf = buf_all[warp];
-    int* perm = perm_all[warp];
+    int const n = d.A.rows, nrhs = d.B.cols, lda = d.A.ld, ldb = d.B.ld;
+    const double* const A = d.A.data;
+    double* const B = d.B.data;
+    const int32_t* const ipiv = d.ipiv;
     const float* F = reinterpret_cast<const float*>(items.ws + d.ws_offset);
     if (info && info[b] != 0) {  // a zero binary32 pivot: no factor to refine with
         for (int c = 0; c < nrhs; ++c)
-            for (int i = lane; i < n; i += 32) d.B.data[i + (int64_t)c * d.B.ld] = CUDART_NAN;
+            for (int i = lane; i < n; i += 32) B[i + (int64_t)c * ldb] = CUDART_NAN;
         if (lane == 0) {
             if (iters) iters[b] = 0;
             if (berr) berr[b] = CUDART_NAN;
@@ -976,7 +996,7 @@ __global__ void __launch_bounds__(kWarps * 32) gesv_mixed_ir_kernel(GesvMixedIte
     __syncwarp();
     if (lane == 0) {
         for (int k = 0; k < n; ++k) {
-            int const q = d.ipiv[k];
+            int const q = ipiv[k];
             if (q != k) {
                 int const t = perm[k];
                 perm[k] = perm[q];
@@ -988,7 +1008,7 @@ __global__ void __launch_bounds__(kWarps * 32) gesv_mixed_ir_kernel(GesvMixedIte
     double anorm = -1.0, worst = 0.0;
     int total_iters = 0;
     for (int c = 0; c < nrhs; ++c) {
-        double* bc = d.B.data + (int64_t)c * d.B.ld;
+        double* bc = B + (int64_t)c * ldb;
         double bv[MAXT], x[MAXT], r[MAXT];
 #pragma unroll
         for (int t = 0; t < MAXT; ++t) bv[t] = lane + 32 * t < n ? bc[lane + 32 * t] : 0.0;
@@ -1014,23 +1034,29 @@ __global__ void __launch_bounds__(kWarps * 32) gesv_mixed_ir_kernel(GesvMixedIte
                 rs[t] = 0.0;
             }
             bool const first = anorm < 0.0;
-            const double* A = d.A.data;
-            double acol[MAXT];
+            // columns of A in four register slots, each reloaded with the column four ahead
+            double acol[4][MAXT];
+            auto load_col = [&](int s, int j) {
 #pragma unroll
-            for (int t = 0; t < MAXT; ++t) acol[t] = lane + 32 * t < n ? A[lane + 32 * t] : 0.0;
-            for (int j = 0; j < n; ++j) {
-                double anx[MAXT];  // column j + 1, loaded before column j's FMAs
-                const double* an = A + (int64_t)(j + 1 < n ? j + 1 : j) * d.A.ld;
+                for (int t = 0; t < MAXT; ++t)
+                    acol[s][t] = (j < n && lane + 32 * t < n) ? A[lane + 32 * t + (int64_t)j * lda] : 0.0;
+            };
 #pragma unroll
-                for (int t = 0; t < MAXT; ++t) anx[t] = lane + 32 * t < n ? an[lane + 32 * t] : 0.0;
-                double const xj = xs[j];
+            for (int s = 0; s < 4; ++s) load_col(s, s);
+            for (int j0 = 0; j0 < n; j0 += 4) {
 #pragma unroll
-                for (int t = 0; t < MAXT; ++t) {
-                    r[t] = fma(-acol[t], xj, r[t]);
-                    if (first) rs[t] += fabs(acol[t]);
+                for (int s = 0; s < 4; ++s) {
+                    int const j = j0 + s;
+                    if (j < n) {
+                        double const xj = xs[j];
+#pragma unroll
+                        for (int t = 0; t < MAXT; ++t) {
+                            r[t] = fma(-acol[s][t], xj, r[t]);
+                            if (first) rs[t] += fabs(acol[s][t]);
+                        }
+                    }
+                    load_col(s, j + 4);
                 }
-#pragma unroll
-                for (int t = 0; t < MAXT; ++t) acol[t] = anx[t];
             }
             __syncwarp();
             if (first) anorm = warp_max_abs<MAXT>(rs, n, lane);
@@ -1058,15 +1084,59 @@ __global__ void __launch_bounds__(kWarps * 32) gesv_mixed_ir_kernel(GesvMixedIte
     }
 }
 
+template <int MAXT>
+__global__ void __launch_bounds__(kWarps * 32) gesv_mixed_ir_kernel(GesvMixedItems items, int64_t count, double tol,
+                                                                   int max_iter, const int32_t* info, int32_t* iters,
+                                                                   double* berr) {
+    __shared__ double xs_all[kWarps][32 * MAXT];
+    __shared__ float buf_all[kWarps][32 * MAXT];
+    __shared__ int perm_all[kWarps][32 * MAXT];
+    int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int64_t const b = (int64_t)blockIdx.x * kWarps + warp;
+    if (b >= count) return;
+    int const n = items.desc[b].A.rows;
+    if (n > 32 * MAXT) return;  // the launch's max_n bounds every instance
+    double* xs = xs_all[warp];
+    float* buf = buf_all[warp];
+    int* perm = perm_all[warp];
+    switch ((n + 31) >> 5) {
+        case 0:
+        case 1: gesv_mixed_ir<1>(items, b, tol, max_iter, info, iters, berr, xs, buf, perm, lane); break;
+        case 2:
+            if constexpr (MAXT >= 2) gesv_mixed_ir<(MAXT >= 2 ? 2 : 1)>(items, b, tol, max_iter, info, iters, berr, xs, buf, perm, lane);
+            break;
+        case 3:
+        case 4:
+            if constexpr (MAXT >= 4) gesv_mixed_ir<(MAXT >= 4 ? 4 : 1)>(items, b, tol, max_iter, info, iters, berr, xs, buf, perm, lane);
+            break;
+        case 5:
+        case 6:
+            if constexpr (MAXT >= 8) gesv_mixed_ir<(MAXT >= 8 ? 6 : 1)>(items, b, tol, max_iter, info, iters, berr, xs, buf, perm, lane);
+            break;
+        default:
+            if constexpr (MAXT >= 8) gesv_mixed_ir<(MAXT >= 8 ? 8 : 1)>(items, b, tol, max_iter, info, iters, berr, xs, buf, perm, lane);
+            break;
+    }
+}
+
 int launch_gesv_mixed(GesvMixedItems items, int64_t count, int max_n, double tol, int max_iter, int32_t* info,
                       int32_t* iters, double* berr, cudaStream_t s) {
     if (count == 0) return BLASTGPU_SUCCESS;
     int64_t const wblocks = (count + kWarps - 1) / kWarps;
     if (wblocks > 0x7fffffff || count > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
     unsigned const wg = (unsigned)wblocks;
-    gesv_mixed_round_kernel<<<wg, kWarps * 32, 0, s>>>(items, count);
-    if (max_n > 64) getrf_cta_f32_kernel<<<(unsigned)count, kCtaThreads, 0, s>>>(items, count, info);
-    else getrf_warp_f32_kernel<<<wg, kWarps * 32, 0, s>>>(items, count, info);
+    gesv_mixed_round_kernel<<<(unsigned)count, kCtaThreads, 0, s>>>(items, count);
+    // "gesv_mixed.lazy": the binary32 factorisation's CTA kernel right-looking (0) or left-looking (1)
+    if (max_n > 64 && tune_get_bin("gesv_mixed.lazy", max_n, 1) != 0) {
+        size_t const smem = sizeof(float) * (size_t)(max_n | 1) * kLazyCols;
+        cudaError_t const e = ensure_smem<getrf_cta_lazy_f32_kernel>(smem);
+        if (e != cudaSuccess) { set_cuda_error(e); return BLASTGPU_ERR_CUDA; }
+        getrf_cta_lazy_f32_kernel<<<(unsigned)count, kCtaThreads, smem, s>>>(items, count, info);
+    } else if (max_n > 64) {
+        getrf_cta_f32_kernel<<<(unsigned)count, kCtaThreads, 0, s>>>(items, count, info);
+    } else {
+        getrf_warp_f32_kernel<<<wg, kWarps * 32, 0, s>>>(items, count, info);
+    }
     int const maxt = (max_n + 31) / 32;
     if (maxt <= 1) gesv_mixed_ir_kernel<1><<<wg, kWarps * 32, 0, s>>>(items, count, tol, max_iter, info, iters, berr);
     else if (maxt <= 2) gesv_mixed_ir_kernel<2><<<wg, kWarps * 32, 0, s>>>(items, count, tol, max_iter, info, iters, berr);
