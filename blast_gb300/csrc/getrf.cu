@@ -331,16 +331,8 @@ constexpr int kLazyCols = 32;
 
 template <typename T>
 __device__ __forceinline__ void lazy_apply_step(T* sp, int ld, int n, int k, int j, const T* L,
-                                                int lda, const int32_t* ipiv, int lane, int kend) {
+                                                int lda, const int32_t* ipiv, int lane) {
     T* col = sp + (int64_t)j * ld;
-    // the next step's block of L (rows k+4 .. n-1 of columns k+4 .. k+7) towards L1 while this
-    // step runs: every step of a column waits on its L loads, and the warps of the CTA read the
-    // same blocks in the same order
-    if (k + 4 < kend) {
-        for (int i = k + 4 + lane; i < n; i += 32)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) asm volatile("prefetch.global.L1 [%0];" ::"l"(L + i + (int64_t)(k + 4 + q) * lda));
-    }
     // swaps of step k (rows k..k+3), one lane
     if (lane == 0) {
 #pragma unroll
@@ -431,7 +423,7 @@ __device__ int cta_getrf_lazy(GetrfItemT<T> it, int* s_ret, T* sp) {
         __syncthreads();
         // every earlier step on this warp's columns (no barrier: the columns are independent)
         for (int c = warp; c < w; c += nwarps)
-            for (int k = 0; k < J; k += NB) lazy_apply_step(sp, ld, n, k, c, a, lda, ipiv, lane, J);
+            for (int k = 0; k < J; k += NB) lazy_apply_step(sp, ld, n, k, c, a, lda, ipiv, lane);
         __syncthreads();
         // the super-panel's own steps
         for (int kk = J; kk < J + w; kk += NB) {
