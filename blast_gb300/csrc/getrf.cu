@@ -870,15 +870,6 @@ __global__ void __launch_bounds__(kCtaThreads) getrf_cta_lazy_f32_kernel(GesvMix
     if (info && threadIdx.x == 0) info[b] = r;
 }
 
-template <int MAXT, typename V>
-__device__ __forceinline__ V pick_t(V const (&v)[MAXT], int t) {
-    V r = (V)0;
-#pragma unroll
-    for (int q = 0; q < MAXT; ++q)
-        if (q == t) r = v[q];
-    return r;
-}
-
 template <int MAXT>
 __device__ __forceinline__ double warp_max_abs(double const (&v)[MAXT], int n, int lane) {
     double m = 0.0;
@@ -899,20 +890,63 @@ __device__ __forceinline__ double warp_max_abs(double const (&v)[MAXT], int n, i
 // lanes over rows (row lane + 32 t in v[t]). perm[i] is the row of v that row i of P v takes
 // (the pivots' interchanges composed), buf: n floats of shared memory. Both substitutions are
 // column sweeps: once an entry is final its lane broadcasts it, and every remaining row takes its
-// term. The factor's columns are read coalesced into four register slots, each reloaded with the
-// column four steps ahead right after use, so a load has three steps to arrive.
+// term. The sweeps run block by block of 32 steps with the block index a compile-time constant
+// (the broadcast entry is v[TL], and the row blocks above or below need no test), and the factor's
+// columns are read coalesced into four register slots, each reloaded with the column four steps
+// ahead right after use.
 template <int MAXT>
 struct ColSlots {
     float v[4][MAXT];
-    // rows lo <= i < hi of column c (zeros elsewhere, or for c outside [0, n))
-    __device__ __forceinline__ void load(int s, const float* F, int n, int c, int lo, int hi, int lane) {
+    // rows i < n of column c, clamped into the matrix (a column outside it is never used)
+    __device__ __forceinline__ void load(int s, const float* F, int n, int c, int lane) {
+        int const cc = c < 0 ? 0 : (c >= n ? n - 1 : c);
 #pragma unroll
         for (int t = 0; t < MAXT; ++t) {
             int const i = lane + 32 * t;
-            v[s][t] = (c >= 0 && c < n && i >= lo && i < hi) ? F[i + (int64_t)c * n] : 0.f;
+            v[s][t] = i < n ? F[i + (int64_t)cc * n] : 0.f;
         }
     }
 };
+
+template <int MAXT, int TL>
+__device__ __forceinline__ void lu_fwd_block(float (&v)[MAXT], ColSlots<MAXT>& cs, const float* F, int n, int lane) {
+    int const lend = min(n - 1, 32 * TL + 32);
+    for (int l0 = 32 * TL; l0 < lend; l0 += 4) {
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+            int const l = l0 + s;
+            if (l < lend) {
+                float const vl = __shfl_sync(0xffffffffu, v[TL], l & 31);
+#pragma unroll
+                for (int t = TL; t < MAXT; ++t)
+                    if (t > TL || lane > (l & 31)) v[t] = fmaf(-cs.v[s][t], vl, v[t]);
+            }
+            cs.load(s, F, n, l + 4, lane);
+        }
+    }
+}
+
+template <int MAXT, int TL>
+__device__ __forceinline__ void lu_bwd_block(float (&v)[MAXT], ColSlots<MAXT>& cs, const float* F, int n, int lane,
+                                             int& l0) {
+    // groups of 4 steps l = l0, l0-1, l0-2, l0-3 with l0 = 3 mod 4 (so that a group never straddles
+    // a 32-step block), down to 32 TL; steps past n - 1 (the top group's) are left out
+    int const lstop = 32 * TL;
+    for (; l0 >= lstop; l0 -= 4) {
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+            int const l = l0 - s;
+            if (l < n) {
+                if (lane == (l & 31)) v[TL] = v[TL] / cs.v[s][TL];
+                float const xl = __shfl_sync(0xffffffffu, v[TL], l & 31);
+#pragma unroll
+                for (int t = 0; t <= TL; ++t)
+                    if (t < TL || lane < (l & 31)) v[t] = fmaf(-cs.v[s][t], xl, v[t]);
+            }
+            cs.load(s, F, n, l - 4, lane);
+        }
+    }
+}
 
 template <int MAXT>
 __device__ void warp_lu_solve_f32(float (&v)[MAXT], const float* F, int n, const int* perm, float* buf, int lane) {
@@ -924,46 +958,29 @@ __device__ void warp_lu_solve_f32(float (&v)[MAXT], const float* F, int n, const
     for (int t = 0; t < MAXT; ++t) v[t] = lane + 32 * t < n ? buf[perm[lane + 32 * t]] : 0.f;
     __syncwarp();
     ColSlots<MAXT> cs;
-    // forward: unit lower; step l uses column l below the diagonal
+    // forward: unit lower; step l uses column l (rows below l take its term)
 #pragma unroll
-    for (int s = 0; s < 4; ++s) cs.load(s, F, n, s, s + 1, n, lane);
-    for (int l0 = 0; l0 < n - 1; l0 += 4) {
+    for (int s = 0; s < 4; ++s) cs.load(s, F, n, s, lane);
+    lu_fwd_block<MAXT, 0>(v, cs, F, n, lane);
+    if constexpr (MAXT > 1) lu_fwd_block<MAXT, (MAXT > 1 ? 1 : 0)>(v, cs, F, n, lane);
+    if constexpr (MAXT > 2) lu_fwd_block<MAXT, (MAXT > 2 ? 2 : 0)>(v, cs, F, n, lane);
+    if constexpr (MAXT > 3) lu_fwd_block<MAXT, (MAXT > 3 ? 3 : 0)>(v, cs, F, n, lane);
+    if constexpr (MAXT > 4) lu_fwd_block<MAXT, (MAXT > 4 ? 4 : 0)>(v, cs, F, n, lane);
+    if constexpr (MAXT > 5) lu_fwd_block<MAXT, (MAXT > 5 ? 5 : 0)>(v, cs, F, n, lane);
+    if constexpr (MAXT > 6) lu_fwd_block<MAXT, (MAXT > 6 ? 6 : 0)>(v, cs, F, n, lane);
+    if constexpr (MAXT > 7) lu_fwd_block<MAXT, (MAXT > 7 ? 7 : 0)>(v, cs, F, n, lane);
+    // backward: upper, dividing by the diagonal; step l uses column l (rows above l take its term)
+    int l0 = ((n - 1) / 4) * 4 + 3;
 #pragma unroll
-        for (int s = 0; s < 4; ++s) {
-            int const l = l0 + s;
-            if (l < n - 1) {
-                float const vl = __shfl_sync(0xffffffffu, pick_t<MAXT>(v, l >> 5), l & 31);
-#pragma unroll
-                for (int t = 0; t < MAXT; ++t) {
-                    int const i = lane + 32 * t;
-                    if (i > l && i < n) v[t] = fmaf(-cs.v[s][t], vl, v[t]);
-                }
-            }
-            cs.load(s, F, n, l + 4, l + 5, n, lane);
-        }
-    }
-    // backward: upper, dividing by the diagonal; step l uses column l on and above the diagonal
-#pragma unroll
-    for (int s = 0; s < 4; ++s) cs.load(s, F, n, n - 1 - s, 0, n - s, lane);
-    for (int l0 = n - 1; l0 >= 0; l0 -= 4) {
-#pragma unroll
-        for (int s = 0; s < 4; ++s) {
-            int const l = l0 - s;
-            if (l >= 0) {
-                // the owner divides its entry by u_ll (slot s holds column l, so its own row's entry is u_ll)
-#pragma unroll
-                for (int t = 0; t < MAXT; ++t)
-                    if (lane + 32 * t == l) v[t] = v[t] / cs.v[s][t];
-                float const xl = __shfl_sync(0xffffffffu, pick_t<MAXT>(v, l >> 5), l & 31);
-#pragma unroll
-                for (int t = 0; t < MAXT; ++t) {
-                    int const i = lane + 32 * t;
-                    if (i < l) v[t] = fmaf(-cs.v[s][t], xl, v[t]);
-                }
-            }
-            cs.load(s, F, n, l - 4, 0, l - 3, lane);
-        }
-    }
+    for (int s = 0; s < 4; ++s) cs.load(s, F, n, l0 - s, lane);
+    if constexpr (MAXT > 7) lu_bwd_block<MAXT, (MAXT > 7 ? 7 : 0)>(v, cs, F, n, lane, l0);
+    if constexpr (MAXT > 6) lu_bwd_block<MAXT, (MAXT > 6 ? 6 : 0)>(v, cs, F, n, lane, l0);
+    if constexpr (MAXT > 5) lu_bwd_block<MAXT, (MAXT > 5 ? 5 : 0)>(v, cs, F, n, lane, l0);
+    if constexpr (MAXT > 4) lu_bwd_block<MAXT, (MAXT > 4 ? 4 : 0)>(v, cs, F, n, lane, l0);
+    if constexpr (MAXT > 3) lu_bwd_block<MAXT, (MAXT > 3 ? 3 : 0)>(v, cs, F, n, lane, l0);
+    if constexpr (MAXT > 2) lu_bwd_block<MAXT, (MAXT > 2 ? 2 : 0)>(v, cs, F, n, lane, l0);
+    if constexpr (MAXT > 1) lu_bwd_block<MAXT, (MAXT > 1 ? 1 : 0)>(v, cs, F, n, lane, l0);
+    lu_bwd_block<MAXT, 0>(v, cs, F, n, lane, l0);
 }
 
 // Refinement, one warp per instance (n <= 32 MAXT): x0 from the binary32 factor, then r = b - A x
@@ -1126,7 +1143,7 @@ int launch_gesv_mixed(GesvMixedItems items, int64_t count, int max_n, double tol
     if (wblocks > 0x7fffffff || count > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
     unsigned const wg = (unsigned)wblocks;
     gesv_mixed_round_kernel<<<(unsigned)count, kCtaThreads, 0, s>>>(items, count);
-    // "gesv_mixed.lazy": the binary32 factorisation's CTA kernel right-looking (0) or left-looking (1)
+    // n > 64: the CTA kernel, left-looking ("gesv_mixed.lazy" = 1, default) or right-looking
     if (max_n > 64 && tune_get_bin("gesv_mixed.lazy", max_n, 1) != 0) {
         size_t const smem = sizeof(float) * (size_t)(max_n | 1) * kLazyCols;
         cudaError_t const e = ensure_smem<getrf_cta_lazy_f32_kernel>(smem);
