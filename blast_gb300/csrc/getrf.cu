@@ -330,50 +330,19 @@ __global__ void __launch_bounds__(kCtaThreads) getrf_cta_kernel(Batch batch, int
 constexpr int kLazyCols = 32;
 
 template <typename T>
-__device__ __forceinline__ void lazy_apply_step(T* sp, int ld, int n, int k, int j, const T* L,
-                                                int lda, const int32_t* ipiv, int lane) {
-    T* col = sp + (int64_t)j * ld;
-    // swaps of step k (rows k..k+3), one lane
-    if (lane == 0) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            int const pr = ipiv[k + q];
-            if (pr != k + q) {
-                T const t = col[k + q];
-                col[k + q] = col[pr];
-                col[pr] = t;
-            }
-        }
-    }
-    __syncwarp();
-    // rows k..k+3 of U (trsm<Lower, unit> with L(k:k+4, k:k+4)), computed by every lane
-    T x[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        T acc = col[k + i];
-#pragma unroll
-        for (int q = 0; q < i; ++q) acc = fma(-L[(k + i) + (int64_t)(k + q) * lda], x[q], acc);
-        x[i] = acc;
-    }
-    __syncwarp();
-    if (lane < 4) col[k + lane] = lane == 0 ? x[0] : lane == 1 ? x[1] : lane == 2 ? x[2] : x[3];
-    // rank-4 update of the rows below, lanes over rows
-    for (int i = k + 4 + lane; i < n; i += 32) {
-        T acc = (T)0;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) acc = fma(L[i + (int64_t)(k + q) * lda], x[q], acc);
-        col[i] = fma((T)1, col[i], -acc);
-    }
-    __syncwarp();
+__device__ __forceinline__ T sel4(T const (&v)[4], int q) {
+    return q == 0 ? v[0] : q == 1 ? v[1] : q == 2 ? v[2] : v[3];
 }
 
-// The same step applied within the super-panel (L block in shared memory, column c of sp).
+// Step k (columns k..k+3 of L, Lk[r + q * ldl] = L(r, k + q)) applied to nc <= 4 columns of the
+// super-panel, c0 + j * cstride for j < nc, by one warp: the columns share the loads of L, and
+// each column's operations are those of BLAST's step in BLAST's order.
 template <typename T>
-__device__ __forceinline__ void lazy_apply_step_smem(T* sp, int ld, int n, int k, int kc, int c,
-                                                     const int32_t* ipiv, int lane) {
-    T* col = sp + (int64_t)c * ld;
-    T const* Lk = sp + (int64_t)kc * ld;  // column k of the matrix is column kc of the super-panel
-    if (lane == 0) {
+__device__ __forceinline__ void lazy_apply_step_cols(T* sp, int ld, int n, int k, int c0, int cstride, int nc,
+                                                     const T* Lk, int ldl, const int32_t* ipiv, int lane) {
+    // swaps of step k (rows k..k+3): lane j < nc swaps column j
+    if (lane < nc) {
+        T* col = sp + (int64_t)(c0 + lane * cstride) * ld;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             int const pr = ipiv[k + q];
@@ -385,21 +354,42 @@ __device__ __forceinline__ void lazy_apply_step_smem(T* sp, int ld, int n, int k
         }
     }
     __syncwarp();
-    T x[4];
+    // rows k..k+3 of U (trsm<Lower, unit> with L(k:k+4, k:k+4)), every lane for every column
+    T const l10 = Lk[(k + 1)], l20 = Lk[(k + 2)], l30 = Lk[(k + 3)];
+    T const l21 = Lk[(k + 2) + (int64_t)ldl], l31 = Lk[(k + 3) + (int64_t)ldl];
+    T const l32 = Lk[(k + 3) + 2 * (int64_t)ldl];
+    T x[4][4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        T acc = col[k + i];
-#pragma unroll
-        for (int q = 0; q < i; ++q) acc = fma(-Lk[(k + i) + (int64_t)q * ld], x[q], acc);
-        x[i] = acc;
+    for (int j = 0; j < 4; ++j) {
+        if (j < nc) {
+            T const* col = sp + (int64_t)(c0 + j * cstride) * ld;
+            x[j][0] = col[k];
+            x[j][1] = fma(-l10, x[j][0], col[k + 1]);
+            x[j][2] = fma(-l21, x[j][1], fma(-l20, x[j][0], col[k + 2]));
+            x[j][3] = fma(-l32, x[j][2], fma(-l31, x[j][1], fma(-l30, x[j][0], col[k + 3])));
+        } else {
+            x[j][0] = x[j][1] = x[j][2] = x[j][3] = (T)0;
+        }
     }
     __syncwarp();
-    if (lane < 4) col[k + lane] = lane == 0 ? x[0] : lane == 1 ? x[1] : lane == 2 ? x[2] : x[3];
-    for (int i = k + 4 + lane; i < n; i += 32) {
-        T acc = (T)0;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) acc = fma(Lk[i + (int64_t)q * ld], x[q], acc);
-        col[i] = fma((T)1, col[i], -acc);
+    for (int j = 0; j < 4; ++j)
+        if (j < nc && lane < 4) sp[(int64_t)(c0 + j * cstride) * ld + k + lane] = sel4(x[j], lane);
+    // rank-4 update of the rows below, lanes over rows
+    for (int i = k + 4 + lane; i < n; i += 32) {
+        T const m0 = Lk[i], m1 = Lk[i + (int64_t)ldl], m2 = Lk[i + 2 * (int64_t)ldl], m3 = Lk[i + 3 * (int64_t)ldl];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (j < nc) {
+                T* col = sp + (int64_t)(c0 + j * cstride) * ld;
+                T acc = (T)0;
+                acc = fma(m0, x[j][0], acc);
+                acc = fma(m1, x[j][1], acc);
+                acc = fma(m2, x[j][2], acc);
+                acc = fma(m3, x[j][3], acc);
+                col[i] = fma((T)1, col[i], -acc);
+            }
+        }
     }
     __syncwarp();
 }
@@ -421,9 +411,14 @@ __device__ int cta_getrf_lazy(GetrfItemT<T> it, int* s_ret, T* sp) {
             sp[(int64_t)c * ld + r] = a[r + (int64_t)(J + c) * lda];
         }
         __syncthreads();
-        // every earlier step on this warp's columns (no barrier: the columns are independent)
-        for (int c = warp; c < w; c += nwarps)
-            for (int k = 0; k < J; k += NB) lazy_apply_step(sp, ld, n, k, c, a, lda, ipiv, lane);
+        // every earlier step on this warp's columns warp, warp + 8, ... (no barrier: the columns
+        // are independent)
+        {
+            int const nc = (w - warp + nwarps - 1) / nwarps;
+            if (nc > 0)
+                for (int k = 0; k < J; k += NB)
+                    lazy_apply_step_cols(sp, ld, n, k, warp, nwarps, nc, a + (int64_t)k * lda, lda, ipiv, lane);
+        }
         __syncthreads();
         // the super-panel's own steps
         for (int kk = J; kk < J + w; kk += NB) {
@@ -439,7 +434,11 @@ __device__ int cta_getrf_lazy(GetrfItemT<T> it, int* s_ret, T* sp) {
             __syncthreads();
             if (*s_ret) return *s_ret;
             if (last) break;
-            for (int c = kc + NB + warp; c < w; c += nwarps) lazy_apply_step_smem(sp, ld, n, kk, kc, c, ipiv, lane);
+            {
+                int const c0 = kc + NB + warp;
+                int const nc = c0 < w ? (w - c0 + nwarps - 1) / nwarps : 0;
+                if (nc > 0) lazy_apply_step_cols(sp, ld, n, kk, c0, nwarps, nc, sp + (int64_t)kc * ld, ld, ipiv, lane);
+            }
             __syncthreads();
         }
         // back to global memory
