@@ -321,9 +321,10 @@ __global__ void __launch_bounds__(kCtaThreads) getrf_cta_kernel(Batch batch, int
 // Mapping: the matrix is processed in super-panels of 32 columns held in shared memory (n x 32
 // doubles, leading dimension n | 1 so that a warp's column accesses spread over the banks). Warp
 // w owns the super-panel's columns c with c % 8 == w. First each warp applies every earlier step
-// to its own columns: swaps, the 4-row solve and the rank-4 update, lanes over rows, the L block of
-// the step read from global memory (all warps read the same rows, so L1 serves them); the columns
-// are independent, so this phase has no barrier. Then the super-panel is factored with BLAST's
+// to its own columns, all of them (up to 4) at once: swaps, the 4-row solve and the rank-4 update,
+// lanes over rows, the L block of the step read from global memory once per row for all the
+// warp's columns (all warps read the same rows, so L1 serves them); the columns are independent,
+// so this phase has no barrier. Then the super-panel is factored with BLAST's
 // inner steps: warp 0 runs getf2 on the 4-column panel in shared memory, and after a barrier every
 // warp applies the step to its own columns right of the panel. The super-panel goes back to global
 // memory, and at the end every column left of a step takes that step's swaps, in step order.
