@@ -256,31 +256,33 @@ __device__ __forceinline__ int potrf_thread(int n, const double* A, Addr ia, dou
 
 constexpr int kRhs = 8;  // right-hand sides per register block of the solves
 
-// Forward solve L*Y = B (Y written to X; X may alias B), register blocks of 4 rows x kRhs.
+// Forward solve L*Y = B (Y written to X; X may alias B), register blocks of 4 rows x RB.
 // Per element: acc = b_ij; for l < i ascending acc = fma(-l_il, y_lj, acc); y_ij = acc * (1/l_ii)
-// (dense/Trsm.hpp:39-52 with the division by l_ii as a multiplication by its reciprocal).
+// (dense/Trsm.hpp:39-52 with the division by l_ii as a multiplication by its reciprocal). The
+// right-hand sides are independent, so RB changes no element's operations.
+template <int RB = kRhs>
 __device__ void trsm_lower_thread(int n, int nrhs, const double* L, int ldl, const double* B, int ldb,
                                   double* X, int ldx) {
-    for (int j0 = 0; j0 < nrhs; j0 += kRhs) {
-        int const nj = min(kRhs, nrhs - j0);
+    for (int j0 = 0; j0 < nrhs; j0 += RB) {
+        int const nj = min(RB, nrhs - j0);
         for (int i0 = 0; i0 < n; i0 += 4) {
             int const ni = min(4, n - i0);
-            double acc[4][kRhs];
+            double acc[4][RB];
 #pragma unroll
             for (int r = 0; r < 4; ++r)
 #pragma unroll
-                for (int c = 0; c < kRhs; ++c)
+                for (int c = 0; c < RB; ++c)
                     acc[r][c] = (r < ni && c < nj) ? B[(i0 + r) + (int64_t)(j0 + c) * ldb] : 0.0;
             for (int l = 0; l < i0; ++l) {
-                double a[4], x[kRhs];
+                double a[4], x[RB];
 #pragma unroll
                 for (int r = 0; r < 4; ++r) a[r] = (r < ni) ? L[(i0 + r) + (int64_t)l * ldl] : 0.0;
 #pragma unroll
-                for (int c = 0; c < kRhs; ++c) x[c] = (c < nj) ? X[l + (int64_t)(j0 + c) * ldx] : 0.0;
+                for (int c = 0; c < RB; ++c) x[c] = (c < nj) ? X[l + (int64_t)(j0 + c) * ldx] : 0.0;
 #pragma unroll
                 for (int r = 0; r < 4; ++r)
 #pragma unroll
-                    for (int c = 0; c < kRhs; ++c) acc[r][c] = fma(-a[r], x[c], acc[r][c]);
+                    for (int c = 0; c < RB; ++c) acc[r][c] = fma(-a[r], x[c], acc[r][c]);
             }
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
@@ -289,45 +291,46 @@ __device__ void trsm_lower_thread(int n, int nrhs, const double* L, int ldl, con
                     for (int q = 0; q < r; ++q) {
                         double const lrq = L[(i0 + r) + (int64_t)(i0 + q) * ldl];
 #pragma unroll
-                        for (int c = 0; c < kRhs; ++c) acc[r][c] = fma(-lrq, acc[q][c], acc[r][c]);
+                        for (int c = 0; c < RB; ++c) acc[r][c] = fma(-lrq, acc[q][c], acc[r][c]);
                     }
                     double const d = rcp_nr(L[(i0 + r) + (int64_t)(i0 + r) * ldl]);
 #pragma unroll
-                    for (int c = 0; c < kRhs; ++c) acc[r][c] *= d;
+                    for (int c = 0; c < RB; ++c) acc[r][c] *= d;
                 }
             }
 #pragma unroll
             for (int r = 0; r < 4; ++r)
 #pragma unroll
-                for (int c = 0; c < kRhs; ++c)
+                for (int c = 0; c < RB; ++c)
                     if (r < ni && c < nj) X[(i0 + r) + (int64_t)(j0 + c) * ldx] = acc[r][c];
         }
     }
 }
 
 // Backward solve L^T*X = Y in place in X (trsm<Upper> on trans(L), dense/Trsm.hpp:53-65).
+template <int RB = kRhs>
 __device__ void trsm_lower_trans_thread(int n, int nrhs, const double* L, int ldl, double* X, int ldx) {
     int const last = ((n - 1) / 4) * 4;
-    for (int j0 = 0; j0 < nrhs; j0 += kRhs) {
-        int const nj = min(kRhs, nrhs - j0);
+    for (int j0 = 0; j0 < nrhs; j0 += RB) {
+        int const nj = min(RB, nrhs - j0);
         for (int i0 = last; i0 >= 0; i0 -= 4) {
             int const ni = min(4, n - i0);
-            double acc[4][kRhs];
+            double acc[4][RB];
 #pragma unroll
             for (int r = 0; r < 4; ++r)
 #pragma unroll
-                for (int c = 0; c < kRhs; ++c)
+                for (int c = 0; c < RB; ++c)
                     acc[r][c] = (r < ni && c < nj) ? X[(i0 + r) + (int64_t)(j0 + c) * ldx] : 0.0;
             for (int l = i0 + 4; l < n; ++l) {
-                double a[4], x[kRhs];
+                double a[4], x[RB];
 #pragma unroll
                 for (int r = 0; r < 4; ++r) a[r] = (r < ni) ? L[l + (int64_t)(i0 + r) * ldl] : 0.0;
 #pragma unroll
-                for (int c = 0; c < kRhs; ++c) x[c] = (c < nj) ? X[l + (int64_t)(j0 + c) * ldx] : 0.0;
+                for (int c = 0; c < RB; ++c) x[c] = (c < nj) ? X[l + (int64_t)(j0 + c) * ldx] : 0.0;
 #pragma unroll
                 for (int r = 0; r < 4; ++r)
 #pragma unroll
-                    for (int c = 0; c < kRhs; ++c) acc[r][c] = fma(-a[r], x[c], acc[r][c]);
+                    for (int c = 0; c < RB; ++c) acc[r][c] = fma(-a[r], x[c], acc[r][c]);
             }
 #pragma unroll
             for (int r = 3; r >= 0; --r) {
@@ -337,18 +340,18 @@ __device__ void trsm_lower_trans_thread(int n, int nrhs, const double* L, int ld
                         if (q < ni) {
                             double const lqr = L[(i0 + q) + (int64_t)(i0 + r) * ldl];
 #pragma unroll
-                            for (int c = 0; c < kRhs; ++c) acc[r][c] = fma(-lqr, acc[q][c], acc[r][c]);
+                            for (int c = 0; c < RB; ++c) acc[r][c] = fma(-lqr, acc[q][c], acc[r][c]);
                         }
                     }
                     double const d = rcp_nr(L[(i0 + r) + (int64_t)(i0 + r) * ldl]);
 #pragma unroll
-                    for (int c = 0; c < kRhs; ++c) acc[r][c] *= d;
+                    for (int c = 0; c < RB; ++c) acc[r][c] *= d;
                 }
             }
 #pragma unroll
             for (int r = 0; r < 4; ++r)
 #pragma unroll
-                for (int c = 0; c < kRhs; ++c)
+                for (int c = 0; c < RB; ++c)
                     if (r < ni && c < nj) X[(i0 + r) + (int64_t)(j0 + c) * ldx] = acc[r][c];
         }
     }
@@ -383,6 +386,182 @@ __global__ void __launch_bounds__(THREADS, MINB) posv_thread_kernel(PosvArgs p) 
         trsm_lower_thread(p.n, p.nrhs, L, p.ldl, p.B + b * p.sb, p.ldb, X, p.ldx);
         trsm_lower_trans_thread(p.n, p.nrhs, L, p.ldl, X, p.ldx);
     }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Quad mode: four lanes per matrix. One thread per matrix fills the chip only when the batch
+// gives every SM sub-partition a few warps (608 sub-partitions: 19,456 matrices a warp each); a
+// smaller batch leaves most of them idle while each of its warps runs the whole serial chain.
+// Quads spread the same batch over four times as many lanes: at n = 48 with 8 right-hand sides,
+// 2,000 matrices take 0.56 ms instead of 1.74 ms, 24,000 take 2.13 ms instead of 2.49 ms; at
+// 50,000 the thread kernel is faster again (4.15 against 4.55 ms: a quad repeats the diagonal
+// block's square roots and the solves' reciprocals for its 4 lanes, and its solve tiles are
+// narrower).
+//
+// Lane g (0..3) of a quad holds rows k + g + 4 j of strip k (j = j0 .. j0 + KM - 1), so that every
+// lane runs the same tile shape and the warp never diverges; the quad's 4 lanes read 4 adjacent
+// rows. Each element sees the operations of the thread-per-matrix tiles in the same order: the
+// fill, the rank-1 updates over l ascending, then the diagonal block's in-register potrf or the
+// trsm against it, and the scaling by the reciprocal square root. DIAG: the strip's first tile
+// (j0 = 0), whose row j = 0 on lane g is row k + g of the 4 x 4 diagonal block; the block's
+// entries reach the other lanes by shuffles within the quad. The strip's later tiles read them
+// from L, as the thread-per-matrix trsm tiles do, and keep y (the reciprocal square roots).
+template <int KM, bool DIAG>
+__device__ __forceinline__ void quad_tile(int n, int k, int nc, int j0, const double* A, int64_t lda, double* L,
+                                          int64_t ldl, int g, unsigned qmask, int qlead, double (&y)[4], int& info) {
+    int const row0 = k + g + 4 * j0;
+    double acc[KM][4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int r = 0; r < KM; ++r) {
+            int const row = row0 + 4 * r;
+            acc[r][c] = (c < nc && row < n) ? A[row + (int64_t)(k + c) * lda] : 0.0;
+        }
+    // acc -= L(rows, 0:k) * L(k:k+4, 0:k)^T, the operands of column l + 1 loaded before the fused
+    // multiply-adds of column l (the row-0 entries above the diagonal are computed and never used)
+    if (k > 0) {
+        double a[KM], b[4];
+#pragma unroll
+        for (int r = 0; r < KM; ++r) a[r] = (row0 + 4 * r < n) ? L[row0 + 4 * r] : 0.0;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) b[c] = (c < nc) ? L[k + c] : 0.0;
+        for (int l = 0; l < k; ++l) {
+            int const ln = l + 1 < k ? l + 1 : l;
+            double an[KM], bn[4];
+#pragma unroll
+            for (int r = 0; r < KM; ++r) an[r] = (row0 + 4 * r < n) ? L[row0 + 4 * r + (int64_t)ln * ldl] : 0.0;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) bn[c] = (c < nc) ? L[(k + c) + (int64_t)ln * ldl] : 0.0;
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+#pragma unroll
+                for (int r = 0; r < KM; ++r) acc[r][c] = fma(-a[r], b[c], acc[r][c]);
+#pragma unroll
+            for (int r = 0; r < KM; ++r) a[r] = an[r];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) b[c] = bn[c];
+        }
+    }
+    if constexpr (DIAG) {
+        // RegisterMatrix::potrf on the block; row j = 0 takes column c's operations if g >= c
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            if (c < nc) {
+#pragma unroll
+                for (int j = 0; j < c; ++j) {
+                    double const lcj = __shfl_sync(qmask, acc[0][j], qlead + c);
+#pragma unroll
+                    for (int r = 0; r < KM; ++r)
+                        if (r > 0 || g >= c) acc[r][c] = fma(-lcj, acc[r][j], acc[r][c]);
+                }
+                double const sc = __shfl_sync(qmask, acc[0][c], qlead + c);
+                if (!(sc > 0.0) && info == 0) info = k + c + 1;
+                y[c] = rsqrt_nr(sc);
+#pragma unroll
+                for (int r = 0; r < KM; ++r)
+                    if (r > 0 || g >= c) acc[r][c] *= y[c];
+            }
+        }
+    } else {
+        // RegisterMatrix::trsm against the block
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            if (c < nc) {
+#pragma unroll
+                for (int j = 0; j < c; ++j) {
+                    double const lcj = L[(k + c) + (int64_t)(k + j) * ldl];
+#pragma unroll
+                    for (int r = 0; r < KM; ++r) acc[r][c] = fma(-lcj, acc[r][j], acc[r][c]);
+                }
+#pragma unroll
+                for (int r = 0; r < KM; ++r) acc[r][c] *= y[c];
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int r = 0; r < KM; ++r) {
+            int const row = row0 + 4 * r;
+            if (c < nc && row < n && (!DIAG || r > 0 || g >= c)) L[row + (int64_t)(k + c) * ldl] = acc[r][c];
+        }
+}
+
+// One tile of KM = rows rounded up to an even count (at most kQuadRows).
+constexpr int kQuadRows = 12;
+
+template <bool DIAG>
+__device__ __forceinline__ void quad_tile_rows(int rows, int n, int k, int nc, int j0, const double* A,
+                                               int64_t lda, double* L, int64_t ldl, int g, unsigned qmask,
+                                               int qlead, double (&y)[4], int& info) {
+    switch ((rows + 1) / 2) {
+        case 1: quad_tile<2, DIAG>(n, k, nc, j0, A, lda, L, ldl, g, qmask, qlead, y, info); break;
+        case 2: quad_tile<4, DIAG>(n, k, nc, j0, A, lda, L, ldl, g, qmask, qlead, y, info); break;
+        case 3: quad_tile<6, DIAG>(n, k, nc, j0, A, lda, L, ldl, g, qmask, qlead, y, info); break;
+        case 4: quad_tile<8, DIAG>(n, k, nc, j0, A, lda, L, ldl, g, qmask, qlead, y, info); break;
+        case 5: quad_tile<10, DIAG>(n, k, nc, j0, A, lda, L, ldl, g, qmask, qlead, y, info); break;
+        default: quad_tile<12, DIAG>(n, k, nc, j0, A, lda, L, ldl, g, qmask, qlead, y, info); break;
+    }
+}
+
+// Left-looking Cholesky of one n x n matrix by a quad (strips of 4 columns, as potrf_thread). Out
+// of line: inlined into the kernel beside the solves, it spilled 460 bytes a thread.
+__device__ __noinline__ int potrf_quad(int n, const double* A, int64_t lda, double* L, int64_t ldl, int g,
+                                       unsigned qmask, int qlead) {
+    int info = 0;
+    for (int k = 0; k < n; k += 4) {
+        int const nc = min(4, n - k);
+        int const rows = (n - k + 3) / 4;  // rows of the strip per lane
+        double y[4];
+        quad_tile_rows<true>(min(rows, kQuadRows), n, k, nc, 0, A, lda, L, ldl, g, qmask, qlead, y, info);
+        if (rows > kQuadRows) {
+            __syncwarp(qmask);  // the diagonal block, stored by its rows' lanes, is read below
+            for (int j0 = kQuadRows; j0 < rows; j0 += kQuadRows)
+                quad_tile_rows<false>(min(rows - j0, kQuadRows), n, k, nc, j0, A, lda, L, ldl, g, qmask, qlead, y,
+                                      info);
+        }
+        __syncwarp(qmask);  // the strip's columns of L, stored by all four lanes, are read next
+    }
+    return info;
+}
+
+// The quad's solves: lane g takes right-hand sides g*q .. g*q + q - 1 (q = ceil(nrhs / 4)).
+__device__ __forceinline__ void potrs_quad(int n, int nrhs, const double* L, int ldl, const double* B, int ldb,
+                                           double* X, int ldx, int g) {
+    int const q = (nrhs + 3) / 4, j0 = g * q, nj = min(q, nrhs - j0);
+    if (nj <= 0) return;
+    const double* Bg = B + (int64_t)j0 * ldb;
+    double* Xg = X + (int64_t)j0 * ldx;
+    if (q <= 1) {
+        trsm_lower_thread<1>(n, nj, L, ldl, Bg, ldb, Xg, ldx);
+        trsm_lower_trans_thread<1>(n, nj, L, ldl, Xg, ldx);
+    } else if (q <= 2) {
+        trsm_lower_thread<2>(n, nj, L, ldl, Bg, ldb, Xg, ldx);
+        trsm_lower_trans_thread<2>(n, nj, L, ldl, Xg, ldx);
+    } else if (q <= 4) {
+        trsm_lower_thread<4>(n, nj, L, ldl, Bg, ldb, Xg, ldx);
+        trsm_lower_trans_thread<4>(n, nj, L, ldl, Xg, ldx);
+    } else {
+        trsm_lower_thread<8>(n, nj, L, ldl, Bg, ldb, Xg, ldx);
+        trsm_lower_trans_thread<8>(n, nj, L, ldl, Xg, ldx);
+    }
+}
+
+// Square matrices only (p.m == 0 or p.m == p.n); 8 matrices per 32-thread CTA.
+__global__ void __launch_bounds__(32, 12) posv_quad_kernel(PosvArgs p) {
+    int const lane = threadIdx.x;
+    int64_t const b = (int64_t)blockIdx.x * 8 + (lane >> 2);
+    if (b >= p.batch) return;  // the whole quad: b depends on lane / 4 only
+    int const g = lane & 3, qlead = lane & ~3;
+    unsigned const qmask = 0xFu << qlead;
+    double* L = p.L + b * p.sl;
+    if (p.mode != 2) {
+        int const info = potrf_quad(p.n, p.A + b * p.sa, p.lda, L, p.ldl, g, qmask, qlead);
+        if (p.info && g == 0) p.info[b] = info;
+    }
+    if (p.mode != 0 && p.nrhs > 0)
+        potrs_quad(p.n, p.nrhs, L, p.ldl, p.B + b * p.sb, p.ldb, p.X + b * p.sx, p.ldx, g);
 }
 
 // Cholesky solve whose inputs and outputs may live in host memory the GPU addresses directly
@@ -543,6 +722,20 @@ __global__ void __launch_bounds__(32, 12) syrk_potrf_thread_kernel(SyrkPotrfArgs
     if (p.info) p.info[b] = info;
 }
 
+// Quads ("posv.quad.n<bin>" = T) when the batch holds fewer than T / 100 full warps per SM
+// sub-partition. Defaults from measurements on GB300 (n = 16: quads win at 8,000 matrices and lose
+// at 16,000; n = 32 and 48, 64: they win up to 24,000 and lose at 50,000); 0 turns them off.
+bool posv_quad_wanted(PosvArgs const& p) {
+    if (p.m != 0 && p.m != p.n) return false;
+    int const def = p.n <= 8 ? 0 : p.n <= 16 ? 50 : p.n <= 64 ? 150 : 100;
+    int const t = tune_get_bin("posv.quad", p.n, def);
+    if (t <= 0) return false;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return false;
+    return p.batch * 100 < (int64_t)t * 32 * 4 * sms;
+}
+
 int launch_posv(PosvArgs const& p, cudaStream_t stream) {
     if (p.batch == 0 || p.n == 0) {
         if (p.info && p.batch > 0 && p.mode != 2) {
@@ -563,6 +756,12 @@ int launch_posv(PosvArgs const& p, cudaStream_t stream) {
     // Measured on GB300 at n = 48 (50,000 instances): 32 threads x 12 CTAs/SM is fastest
     // (4.29 ms vs 4.56 ms for 64 x 6 and 5.30 ms for 64 x 1); it lets the block scheduler even
     // out the per-SM load one warp at a time.
+    if (posv_quad_wanted(p)) {
+        int64_t const qblocks = (p.batch + 7) / 8;
+        if (qblocks > 0x7fffffff) return BLASTGPU_ERR_TOO_LARGE;
+        posv_quad_kernel<<<(unsigned)qblocks, 32, 0, stream>>>(p);
+        return check_launch();
+    }
     int const variant = tune_get_bin("posv.variant", p.n, 3);
     int const threads = variant == 2 ? 128 : (variant == 3 || variant == 4) ? 32 : 64;
     int64_t const blocks = (p.batch + threads - 1) / threads;

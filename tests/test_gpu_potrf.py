@@ -143,3 +143,47 @@ def test_potrf_size_errors(gpu):
     dL = gpu.col_major((2,), 3, 3, "cuda")
     with pytest.raises(ValueError):
         gpu.potrf(dA, dL)
+
+
+@pytest.mark.parametrize("n,nrhs,batch", [(48, 8, 20_000), (48, 8, 2_000), (13, 3, 777), (61, 13, 1_000),
+                                          (100, 8, 300), (1, 1, 50), (4, 2, 40)])
+def test_posv_quad_kernel_bit_identical(gpu, n, nrhs, batch):
+    """The quad kernel (4 lanes per matrix, rows interleaved over the lanes, right-hand sides split
+    between them; ``posv.quad.n<bin>`` chooses it by batch size) gives the thread-per-matrix
+    kernel's L, X and info bit for bit, for posv, potrf and potrs: every element sees the same
+    operations in the same order. n = 61 and 100 take more than one tile of rows per lane."""
+    import torch
+
+    from blast_gb300 import _lib
+    from blast_gb300.tune import size_bin
+
+    rng = np.random.default_rng(n * 1000 + nrhs)
+    A = spd_batch(rng, batch, n)
+    A[batch // 2, n // 2, n // 2] = -1.0  # one matrix not positive definite: info and NaNs agree
+    B = rng.standard_normal((batch, n, nrhs))
+    key = f"posv.quad.n{size_bin(n)}"
+    old = _lib.tune_get(key)
+    outs = {}
+    try:
+        for q in (0, 1_000_000):  # never / always quads
+            _lib.tune_set(key, q)
+            dA, dB = to_dev(A), to_dev(B)
+            dL = gpu.col_major((batch,), n, n, "cuda")
+            dL.zero_()
+            dX = gpu.col_major((batch,), n, nrhs, "cuda")
+            info = gpu.posv(dA, dL, dB, dX)
+            dL2 = gpu.col_major((batch,), n, n, "cuda")
+            dL2.zero_()
+            info2 = gpu.potrf(dA, dL2)
+            dY = to_dev(B)
+            gpu.potrs(dL2, dY, dY)
+            torch.cuda.synchronize()
+            outs[q] = [t.cpu().numpy() for t in (dL, dX, info, dL2, info2, dY)]
+    finally:
+        if old is not None:
+            _lib.tune_set(key, old)
+        else:
+            _lib.tune_set(key, 0 if n <= 8 else 50 if n <= 16 else 150 if n <= 64 else 100)
+    assert outs[0][2][batch // 2] != 0
+    for a, b in zip(outs[0], outs[1_000_000]):
+        assert np.array_equal(a, b, equal_nan=True)
