@@ -764,6 +764,42 @@ def workload_riccati(args):
 # ---------------------------------------------------------------------------------------------
 # The GPU arm
 # ---------------------------------------------------------------------------------------------
+def workload_posv_batches(args) -> dict:
+    """Cholesky solves n = 48 with 8 right-hand sides (A = G G^T + 48 I, B ~ N(0,1)) at batch sizes
+    from 500 to 50,000: the library's launch choice (one thread per matrix, or a quad of lanes per
+    matrix for batches that hold fewer than 1.5 full warps per SM sub-partition) against the
+    thread-per-matrix kernel alone ("posv.quad" = 0), with the two results compared bit for bit."""
+    import numpy as np
+    import torch
+
+    import blast_gb300 as bg
+    from blast_gb300 import _lib
+
+    dev = torch.device("cuda", 0)
+    key = "posv.quad.n64"
+    default = _lib.tune_get(key)
+    rows = []
+    for batch in (500, 2_000, 8_000, 16_000, 24_000, 50_000):
+        A_h, B_h = host_inputs(batch, SEED)
+        A, B = _to_dev_batch(A_h, dev), _to_dev_batch(B_h, dev)
+        L = bg.col_major((batch,), N, N, dev)
+        X = bg.col_major((batch,), N, NRHS, dev)
+        row = {"batch": batch}
+        outs = {}
+        for name, q in (("library", default), ("thread_kernel", 0)):
+            if q is None:
+                q = 150
+            _lib.tune_set(key, q)
+            row[f"{name}_ms"] = _timed(lambda: bg.posv(A, L, B, X), args.steps)
+            outs[name] = (L.cpu().numpy(), X.cpu().numpy())
+        _lib.tune_set(key, 150 if default is None else default)
+        row["speedup"] = row["thread_kernel_ms"] / row["library_ms"]
+        row["bit_identical"] = all(np.array_equal(a, b) for a, b in zip(outs["library"], outs["thread_kernel"]))
+        rows.append(row)
+        del A, B, L, X
+    return {"workload": "posv n = 48, 8 RHS, batch 500 .. 50,000", "steps": args.steps, "rows": rows}
+
+
 def _traffic_from_profile(batch: int):
     p = ROOT / "profiles" / "posv_thread_n48_traffic.json"
     try:
@@ -1001,7 +1037,7 @@ def main():
     ap.add_argument("--batch", type=int, default=BATCH, help="matrices per GPU (default 50,000)")
     ap.add_argument("--no-mixed", action="store_true",
                     help="skip the FP64-vs-mixed comparison on the ragged n in [64, 512] batch")
-    ap.add_argument("--workload", choices=["cholesky48", "gemm24", "lu_ragged", "adjoint", "riccati"],
+    ap.add_argument("--workload", choices=["cholesky48", "gemm24", "lu_ragged", "adjoint", "riccati", "posv_batches"],
                     default="cholesky48", help="cholesky48 (default) prints the contract line; the "
                     "others print one JSON object for that workload alone")
     ap.add_argument("--count", type=int, default=0,
@@ -1039,6 +1075,8 @@ def main():
             res = config_lu_ragged(args.steps, peak, count=args.count or 20_000, cpu=not args.no_cpu)
         elif args.workload == "adjoint":
             res = config_adjoint(args.steps, peak)
+        elif args.workload == "posv_batches":
+            res = workload_posv_batches(args)
         else:
             res = workload_riccati(args)
         print(json.dumps(res), flush=True)
