@@ -724,10 +724,11 @@ __global__ void __launch_bounds__(32, 12) syrk_potrf_thread_kernel(SyrkPotrfArgs
 
 // Quads ("posv.quad.n<bin>" = T) when the batch holds fewer than T / 100 full warps per SM
 // sub-partition. Defaults from measurements on GB300 (n = 16: quads win at 8,000 matrices and lose
-// at 16,000; n = 32 and 48, 64: they win up to 24,000 and lose at 50,000); 0 turns them off.
+// at 16,000; n = 32, 48 and 64: they win up to 24,000 and lose at 50,000; n = 96 and 128: 3.3-3.7x
+// at 2,000 and 8,000, 1.6x at 16,000); 0 turns them off.
 bool posv_quad_wanted(PosvArgs const& p) {
     if (p.m != 0 && p.m != p.n) return false;
-    int const def = p.n <= 8 ? 0 : p.n <= 16 ? 50 : p.n <= 64 ? 150 : 100;
+    int const def = p.n <= 8 ? 0 : p.n <= 16 ? 50 : 150;
     int const t = tune_get_bin("posv.quad", p.n, def);
     if (t <= 0) return false;
     int dev = 0, sms = 0;

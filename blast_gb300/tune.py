@@ -20,7 +20,7 @@ Tunable choices (read by the library through blastgpu_tune_set / tune_get_bin):
   CTA (0) per matrix (same bits as the thread kernel, or within 10 n eps of it).
 * ``posv.quad.n<bin>`` — uniform Cholesky batches (thread-per-matrix sizes) run a quad of lanes per
   matrix when they hold fewer than value / 100 full warps per SM sub-partition (same bits; not
-  timed by this module: the library's defaults, 0 / 50 / 150 / 150 / 150 / 100 for the bins 8 to
+  timed by this module: the library's defaults, 0 / 50 / 150 / 150 / 150 / 150 for the bins 8 to
   128, come from ``bench.py --workload posv_batches`` style measurements).
 
 Results are cached as JSON keyed by GPU name (``blast_gb300/tuning/<gpu>.json``); ``apply()``

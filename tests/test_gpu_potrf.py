@@ -183,7 +183,7 @@ def test_posv_quad_kernel_bit_identical(gpu, n, nrhs, batch):
         if old is not None:
             _lib.tune_set(key, old)
         else:
-            _lib.tune_set(key, 0 if n <= 8 else 50 if n <= 16 else 150 if n <= 64 else 100)
+            _lib.tune_set(key, 0 if n <= 8 else 50 if n <= 16 else 150)
     assert outs[0][2][batch // 2] != 0
     for a, b in zip(outs[0], outs[1_000_000]):
         assert np.array_equal(a, b, equal_nan=True)
