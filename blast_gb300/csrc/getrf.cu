@@ -376,9 +376,16 @@ __device__ __forceinline__ void lazy_apply_step_cols(T* sp, int ld, int n, int k
 #pragma unroll
     for (int j = 0; j < 4; ++j)
         if (j < nc && lane < 4) sp[(int64_t)(c0 + j * cstride) * ld + k + lane] = sel4(x[j], lane);
-    // rank-4 update of the rows below, lanes over rows
-    for (int i = k + 4 + lane; i < n; i += 32) {
-        T const m0 = Lk[i], m1 = Lk[i + (int64_t)ldl], m2 = Lk[i + 2 * (int64_t)ldl], m3 = Lk[i + 3 * (int64_t)ldl];
+    // rank-4 update of the rows below, lanes over rows; the next row's L values are loaded before
+    // this row's stores to the super-panel (which the loads could otherwise be held behind)
+    int i = k + 4 + lane;
+    T m0 = (T)0, m1 = (T)0, m2 = (T)0, m3 = (T)0;
+    if (i < n) m0 = Lk[i], m1 = Lk[i + (int64_t)ldl], m2 = Lk[i + 2 * (int64_t)ldl], m3 = Lk[i + 3 * (int64_t)ldl];
+    for (; i < n; i += 32) {
+        int const in = i + 32;
+        T p0 = (T)0, p1 = (T)0, p2 = (T)0, p3 = (T)0;
+        if (in < n)
+            p0 = Lk[in], p1 = Lk[in + (int64_t)ldl], p2 = Lk[in + 2 * (int64_t)ldl], p3 = Lk[in + 3 * (int64_t)ldl];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             if (j < nc) {
@@ -391,6 +398,7 @@ __device__ __forceinline__ void lazy_apply_step_cols(T* sp, int ld, int n, int k
                 col[i] = fma((T)1, col[i], -acc);
             }
         }
+        m0 = p0, m1 = p1, m2 = p2, m3 = p3;
     }
     __syncwarp();
 }
