@@ -308,8 +308,8 @@ int blastgpu_dgetrs_batched(const blastgpu_getrf_desc* desc, const int32_t* info
 int blastgpu_dgesv_batched(const blastgpu_getrf_desc* desc, int32_t* info, int64_t batch,
                            int max_n, blastgpu_stream_t stream);
 
-/* Mixed-precision LU solve with iterative refinement (no BLAST counterpart; the benchmark spec's
- * mixed form applied to getrf/getrs): per instance, A (binary64, read only) is rounded to
+/* Mixed-precision LU solve with iterative refinement (no BLAST counterpart; the mixed-precision
+ * form of blastgpu_dposv_mixed_batched applied to getrf/getrs): per instance, A (binary64, read only) is rounded to
  * binary32 in the caller's workspace and factored there by the same blocked partial-pivoting
  * algorithm as blastgpu_dgetrf_batched; X := A^{-1} B (B overwritten) is then refined in binary64
  * (r = b - A x, correction solved with the binary32 factor on r / |r|_inf) until the normwise
