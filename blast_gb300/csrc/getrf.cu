@@ -256,18 +256,38 @@ __device__ int cta_getrf(GetrfItemT<T> it, int* s_ret, T* sp) {
             }
         }
         __syncthreads();
-        // A22 := A22 - A21 * U12, thread per row
+        // A22 := A22 - A21 * U12, thread per row. Column j + 1's operands (U12, final in this
+        // phase, and this thread's own element) are loaded before column j's store, which they
+        // would otherwise wait behind (the compiler cannot tell the addresses apart).
         for (int i = k + NB + tid; i < M; i += kCtaThreads) {
             T l[NB];
 #pragma unroll
             for (int q = 0; q < NB; ++q) l[q] = a[i + (int64_t)(k + q) * lda];
-            for (int j = k + NB; j < N; ++j) {
-                T const* u = a + k + (int64_t)j * lda;
+            int j = k + NB;
+            T u[NB], cv = (T)0;
+#pragma unroll
+            for (int q = 0; q < NB; ++q) u[q] = (T)0;
+            if (j < N) {
+#pragma unroll
+                for (int q = 0; q < NB; ++q) u[q] = a[k + q + (int64_t)j * lda];
+                cv = a[i + (int64_t)j * lda];
+            }
+            for (; j < N; ++j) {
+                T un[NB], cn = (T)0;
+#pragma unroll
+                for (int q = 0; q < NB; ++q) un[q] = (T)0;
+                if (j + 1 < N) {
+#pragma unroll
+                    for (int q = 0; q < NB; ++q) un[q] = a[k + q + (int64_t)(j + 1) * lda];
+                    cn = a[i + (int64_t)(j + 1) * lda];
+                }
                 T acc = (T)0;
 #pragma unroll
                 for (int q = 0; q < NB; ++q) acc = fma(l[q], u[q], acc);
-                T* c = a + i + (int64_t)j * lda;
-                *c = fma((T)1, *c, -acc);
+                a[i + (int64_t)j * lda] = fma((T)1, cv, -acc);
+#pragma unroll
+                for (int q = 0; q < NB; ++q) u[q] = un[q];
+                cv = cn;
             }
         }
         __syncthreads();
